@@ -1,0 +1,391 @@
+// api.cu - the extern "C" boundary (include/sjbg.h) and the handle runtime.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "eager.cuh"
+#include "runtime.h"
+#include "stream.cuh"
+
+namespace {
+std::mutex g_err_mu;
+std::string g_create_err;
+}  // namespace
+
+sjbg_handle::~sjbg_handle() {
+    if (device >= 0) cudaSetDevice(device);
+    eager.reset();
+    streaming.reset();
+    for (auto &b : ws)
+        if (b.p) cudaFree(b.p);
+    for (auto &b : pinned)
+        if (b.p) cudaFreeHost(b.p);
+    for (auto &p : pending) {
+        event_pool.push_back(p.a);
+        event_pool.push_back(p.b);
+    }
+    for (auto e : event_pool) cudaEventDestroy(e);
+    if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+namespace sjbg {
+
+int fail(sjbg_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    else {
+        std::lock_guard<std::mutex> g(g_err_mu);
+        g_create_err = msg;
+    }
+    return code;
+}
+
+int cuda_fail(sjbg_handle *h, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(h, e == cudaErrorMemoryAllocation ? SJBG_E_NOMEM : SJBG_E_CUDA, m);
+}
+
+void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes) {
+    DevBuf &b = h->ws[s];
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return b.p;
+    if (b.p) {
+        cudaStreamSynchronize(h->stream);   // a kernel may still use the old buffer
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = std::max(bytes, b.bytes + b.bytes / 4);
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+        cudaGetLastError();
+        if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            b.p = nullptr;
+            return nullptr;
+        }
+        want = bytes;
+    }
+    b.bytes = want;
+    return b.p;
+}
+
+void *pinned_get(sjbg_handle *h, int i, size_t bytes) {
+    DevBuf &b = h->pinned[i];
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return b.p;
+    if (b.p) {
+        cudaStreamSynchronize(h->stream);
+        cudaFreeHost(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = std::max(bytes, (size_t)4096);
+    if (cudaMallocHost(&b.p, want) != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        return nullptr;
+    }
+    b.bytes = want;
+    return b.p;
+}
+
+int kernel_id(sjbg_handle *h, const char *name) {
+    for (size_t i = 0; i < h->knames.size(); i++)
+        if (h->knames[i] == name) return (int)i;
+    h->knames.emplace_back(name);
+    h->klaunches.push_back(0);
+    h->kms.push_back(0.0);
+    return (int)h->knames.size() - 1;
+}
+
+cudaEvent_t event_get(sjbg_handle *h) {
+    if (!h->event_pool.empty()) {
+        cudaEvent_t e = h->event_pool.back();
+        h->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void profile_collect(sjbg_handle *h) {
+    for (auto &p : h->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            h->klaunches[p.kid]++;
+            h->kms[p.kid] += ms;
+        }
+        h->event_pool.push_back(p.a);
+        h->event_pool.push_back(p.b);
+    }
+    h->pending.clear();
+}
+
+// ---- lazy batches ---------------------------------------------------------------
+static bool wants_pairs(const sjbg_handle *h) { return h->cfg.result_mode != SJBG_RESULT_NO_OUTPUT; }
+
+// Run windows whose spans index device arrays dL / dR; dPairs (device) may be null.
+static int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                           sjbg_pair *dPairs, WinAcc *hAcc, uint32_t *part_used) {
+    const bool pairs = dPairs != nullptr;
+    const bool enumerate = pairs || (h->cfg.flags & SJBG_F_XOR);
+    WinAcc *acc = static_cast<WinAcc *>(ws_get(h, WS_WIN_ACC, sizeof(WinAcc) * n));
+    if (!acc) return fail(h, SJBG_E_NOMEM, "window accumulators");
+    SJBG_CK(h, cudaMemsetAsync(acc, 0, sizeof(WinAcc) * n, h->stream));
+    int rc = SJBG_OK;
+    *part_used = SJBG_PART_NONE;
+    switch (h->cfg.algorithm) {
+        case SJBG_ALG_HJ: rc = hj_lazy_batch(h, dL, dR, wins, n, dPairs, acc, enumerate, part_used); break;
+        case SJBG_ALG_NLJ: rc = nlj_lazy_batch(h, dL, dR, wins, n, dPairs, acc, enumerate); break;
+        case SJBG_ALG_SMJ: rc = smj_lazy_batch(h, dL, dR, wins, n, dPairs, acc, enumerate); break;
+        default: rc = fail(h, SJBG_E_UNSUPPORTED, "unknown algorithm");
+    }
+    if (rc) return rc;
+    SJBG_CK(h, cudaMemcpyAsync(hAcc, acc, sizeof(WinAcc) * n, cudaMemcpyDeviceToHost, h->stream));
+    return SJBG_OK;
+}
+
+static void fill_result(const sjbg_handle *h, const WinAcc &a, const WinHost &w, bool enumerate, bool pairs,
+                        uint32_t part_used, float ms, sjbg_window_result *out) {
+    std::memset(out, 0, sizeof(*out));
+    out->count = a.count;
+    out->prod_checksum = a.prod;
+    out->partitioner_used = part_used;
+    out->ms = ms;
+    if (enumerate) {
+        out->xor_checksum = a.xr;
+        out->flags |= SJBG_WR_XOR;
+    }
+    if (pairs) {
+        out->n_pairs = std::min<uint64_t>(a.npairs, w.pairs_cap);
+        if (a.npairs > w.pairs_cap) out->flags |= SJBG_WR_PAIRS_TRUNCATED;
+    }
+    (void)h;
+}
+
+int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32_t mem, const WinHost *wins,
+                uint32_t n, sjbg_pair *pairs, sjbg_window_result *out) {
+    if (!h) return SJBG_E_INVALID;
+    if (h->cfg.progressiveness != SJBG_LAZY) return fail(h, SJBG_E_STATE, "lazy call on an eager handle");
+    if (mem != SJBG_MEM_HOST && mem != SJBG_MEM_DEVICE) return fail(h, SJBG_E_INVALID, "bad memory kind");
+    if (n && !wins) return fail(h, SJBG_E_INVALID, "null window list");
+    if (!out) return fail(h, SJBG_E_INVALID, "null result");
+    SJBG_CK(h, cudaSetDevice(h->device));
+    uint64_t needL = 0, needR = 0, needP = 0;
+    for (uint32_t w = 0; w < n; w++) {
+        if (wins[w].n_left > h->cfg.max_tuples_per_window || wins[w].n_right > h->cfg.max_tuples_per_window)
+            return fail(h, SJBG_E_CAPACITY, "window larger than max_tuples_per_window");
+        needL = std::max(needL, wins[w].left_off + wins[w].n_left);
+        needR = std::max(needR, wins[w].right_off + wins[w].n_right);
+        needP = std::max(needP, wins[w].pairs_off + wins[w].pairs_cap);
+    }
+    if ((needL && !L) || (needR && !R)) return fail(h, SJBG_E_INVALID, "null input span");
+    const bool want = wants_pairs(h) && pairs != nullptr && needP > 0;
+    const bool enumerate = want || (h->cfg.flags & SJBG_F_XOR);
+
+    cudaEvent_t e0 = event_get(h), e1 = event_get(h);
+    SJBG_CK(h, cudaEventRecord(e0, h->stream));
+    const sjbg_tuple *dL = L, *dR = R;
+    sjbg_pair *dP = want ? pairs : nullptr;
+    if (mem == SJBG_MEM_HOST) {
+        sjbg_tuple *sL = static_cast<sjbg_tuple *>(ws_get(h, WS_IN_LEFT, sizeof(sjbg_tuple) * needL));
+        sjbg_tuple *sR = static_cast<sjbg_tuple *>(ws_get(h, WS_IN_RIGHT, sizeof(sjbg_tuple) * needR));
+        if (!sL || !sR) return fail(h, SJBG_E_NOMEM, "input staging");
+        if (needL) SJBG_CK(h, cudaMemcpyAsync(sL, L, sizeof(sjbg_tuple) * needL, cudaMemcpyHostToDevice, h->stream));
+        if (needR) SJBG_CK(h, cudaMemcpyAsync(sR, R, sizeof(sjbg_tuple) * needR, cudaMemcpyHostToDevice, h->stream));
+        dL = sL;
+        dR = sR;
+        if (want) {
+            dP = static_cast<sjbg_pair *>(ws_get(h, WS_PAIRS, sizeof(sjbg_pair) * needP));
+            if (!dP) return fail(h, SJBG_E_NOMEM, "pair staging");
+        }
+    }
+    // CountKernel mode: an exact count first; refuse instead of truncating
+    if (want && h->cfg.result_mode == SJBG_RESULT_COUNT_KERNEL) {
+        WinAcc *hp = static_cast<WinAcc *>(pinned_get(h, 4, sizeof(WinAcc) * n));
+        if (!hp) return fail(h, SJBG_E_NOMEM, "count staging");
+        uint32_t pu;
+        int rc = run_lazy_device(h, dL, dR, wins, n, nullptr, hp, &pu);
+        if (rc) return rc;
+        SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        for (uint32_t w = 0; w < n; w++)
+            if (hp[w].count > wins[w].pairs_cap)
+                return fail(h, SJBG_E_CAPACITY, "pair buffer smaller than the window's match count");
+    }
+    WinAcc *hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * std::max<uint32_t>(n, 1)));
+    if (!hAcc) return fail(h, SJBG_E_NOMEM, "result staging");
+    uint32_t part_used = SJBG_PART_NONE;
+    int rc = run_lazy_device(h, dL, dR, wins, n, dP, hAcc, &part_used);
+    if (rc) return rc;
+    if (mem == SJBG_MEM_HOST && want) {
+        // copy back each window's written pairs
+        SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        for (uint32_t w = 0; w < n; w++) {
+            const uint64_t np = std::min<uint64_t>(hAcc[w].npairs, wins[w].pairs_cap);
+            if (np)
+                SJBG_CK(h, cudaMemcpyAsync(pairs + wins[w].pairs_off, dP + wins[w].pairs_off, sizeof(sjbg_pair) * np,
+                                           cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    SJBG_CK(h, cudaEventRecord(e1, h->stream));
+    SJBG_CK(h, cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    h->event_pool.push_back(e0);
+    h->event_pool.push_back(e1);
+    profile_collect(h);
+    for (uint32_t w = 0; w < n; w++) fill_result(h, hAcc[w], wins[w], enumerate, want, part_used, ms, &out[w]);
+    return SJBG_OK;
+}
+
+}  // namespace sjbg
+
+using namespace sjbg;
+
+extern "C" {
+
+int sjbg_version(void) { return SJBG_ABI_VERSION; }
+
+int sjbg_create(const sjbg_config *cfg, sjbg_handle **out) {
+    if (!cfg || !out) return fail(nullptr, SJBG_E_INVALID, "null argument");
+    *out = nullptr;
+    if (cfg->algorithm != SJBG_ALG_HJ && cfg->algorithm != SJBG_ALG_NLJ && cfg->algorithm != SJBG_ALG_SMJ)
+        return fail(nullptr, SJBG_E_UNSUPPORTED, "algorithm must be NLJ, HJ or SMJ");
+    if (cfg->progressiveness != SJBG_LAZY && cfg->progressiveness != SJBG_EAGER)
+        return fail(nullptr, SJBG_E_INVALID, "progressiveness must be LAZY or EAGER");
+    if (cfg->result_mode > SJBG_RESULT_ATOMIC) return fail(nullptr, SJBG_E_INVALID, "bad result mode");
+    if (cfg->partitioner > SJBG_PART_LEARNED) return fail(nullptr, SJBG_E_INVALID, "bad partitioner");
+    if (cfg->radix_bits > 14) return fail(nullptr, SJBG_E_INVALID, "radix_bits must be <= 14");
+    if (cfg->max_tuples_per_window == 0) return fail(nullptr, SJBG_E_INVALID, "max_tuples_per_window must be > 0");
+    if (cfg->progressiveness == SJBG_EAGER && (cfg->batch_size == 0 || cfg->window_size == 0))
+        return fail(nullptr, SJBG_E_INVALID, "eager handles need batch_size and window_size");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, SJBG_E_CUDA, "no CUDA device available");
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return fail(nullptr, SJBG_E_INVALID, "bad device ordinal");
+    std::unique_ptr<sjbg_handle> h(new sjbg_handle());
+    h->cfg = *cfg;
+    if (h->cfg.partitioner == SJBG_PART_AUTO) h->cfg.partitioner = SJBG_PART_RADIX;
+    h->device = cfg->device;
+    if ((e = cudaSetDevice(h->device)) != cudaSuccess) return fail(nullptr, SJBG_E_CUDA, cudaGetErrorString(e));
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    h->max_smem_optin = (size_t)optin;
+    if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail(nullptr, SJBG_E_CUDA, cudaGetErrorString(e));
+    h->stream = h->own_stream;
+    if (cfg->progressiveness == SJBG_EAGER) {
+        int rc = eager_init(h.get());
+        if (rc) {
+            std::lock_guard<std::mutex> g(g_err_mu);
+            g_create_err = h->err;
+            return rc;
+        }
+    }
+    *out = h.release();
+    return SJBG_OK;
+}
+
+int sjbg_destroy(sjbg_handle *h) {
+    if (!h) return SJBG_E_INVALID;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+    return SJBG_OK;
+}
+
+const char *sjbg_last_error(const sjbg_handle *h) {
+    if (h) return h->err.c_str();
+    std::lock_guard<std::mutex> g(g_err_mu);
+    return g_create_err.c_str();
+}
+
+int sjbg_set_stream(sjbg_handle *h, void *cuda_stream) {
+    if (!h) return SJBG_E_INVALID;
+    h->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->own_stream;
+    return SJBG_OK;
+}
+
+int sjbg_lazy_execute(sjbg_handle *h, const sjbg_tuple *left, uint64_t n_left, const sjbg_tuple *right,
+                      uint64_t n_right, uint32_t mem, sjbg_pair *pairs, uint64_t pairs_capacity,
+                      sjbg_window_result *out) {
+    WinHost w{0, n_left, 0, n_right, 0, pairs ? pairs_capacity : 0};
+    return lazy_common(h, left, right, mem, &w, 1, pairs, out);
+}
+
+int sjbg_lazy_execute_ring(sjbg_handle *h, const sjbg_tuple *left_ring, const uint64_t *left_batch_offsets,
+                           uint64_t n_left_batches, const sjbg_tuple *right_ring, const uint64_t *right_batch_offsets,
+                           uint64_t n_right_batches, sjbg_pair *pairs, uint64_t pairs_capacity,
+                           sjbg_window_result *out) {
+    if (!h) return SJBG_E_INVALID;
+    const uint64_t B = h->cfg.batch_size;
+    if (B == 0) return fail(h, SJBG_E_INVALID, "batch_size must be set for ring windows");
+    if ((n_left_batches && (!left_ring || !left_batch_offsets)) ||
+        (n_right_batches && (!right_ring || !right_batch_offsets)))
+        return fail(h, SJBG_E_INVALID, "null ring or offsets");
+    // gather the window's batches into contiguous pinned spans (the reference's
+    // copyTuplesToLocalStore assumes contiguity, GPU_HJ.cu:237-242)
+    const uint64_t nL = n_left_batches * B, nR = n_right_batches * B;
+    sjbg_tuple *g = static_cast<sjbg_tuple *>(pinned_get(h, 2, sizeof(sjbg_tuple) * (nL + nR)));
+    if (!g) return fail(h, SJBG_E_NOMEM, "ring gather buffer");
+    for (uint64_t i = 0; i < n_left_batches; i++)
+        std::memcpy(g + i * B, left_ring + left_batch_offsets[i], sizeof(sjbg_tuple) * B);
+    for (uint64_t i = 0; i < n_right_batches; i++)
+        std::memcpy(g + nL + i * B, right_ring + right_batch_offsets[i], sizeof(sjbg_tuple) * B);
+    WinHost w{0, nL, 0, nR, 0, pairs ? pairs_capacity : 0};
+    return lazy_common(h, g, g + nL, SJBG_MEM_HOST, &w, 1, pairs, out);
+}
+
+int sjbg_lazy_execute_batch(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *right, uint32_t mem,
+                            const sjbg_window_desc *windows, uint32_t n_windows, sjbg_pair *pairs,
+                            sjbg_window_result *out) {
+    if (!h) return SJBG_E_INVALID;
+    std::vector<WinHost> w(n_windows);
+    for (uint32_t i = 0; i < n_windows; i++) {
+        const sjbg_window_desc &d = windows[i];
+        w[i] = WinHost{d.left_offset, d.n_left, d.right_offset, d.n_right, d.pairs_offset,
+                       pairs ? d.pairs_capacity : 0};
+    }
+    return lazy_common(h, left, right, mem, w.data(), n_windows, pairs, out);
+}
+
+int sjbg_generate(sjbg_handle *h, sjbg_tuple *dev_out, uint64_t first, uint64_t n, uint64_t seed, uint64_t domain,
+                  const uint64_t *zipf_table, uint64_t perm_seed) {
+    if (!h || (!dev_out && n)) return SJBG_E_INVALID;
+    if (domain == 0 || domain > (1ull << 32)) return fail(h, SJBG_E_INVALID, "domain must be in [1, 2^32]");
+    SJBG_CK(h, cudaSetDevice(h->device));
+    int rc = generate_device(h, dev_out, first, n, seed, domain, zipf_table, perm_seed);
+    if (rc) return rc;
+    SJBG_CK(h, cudaStreamSynchronize(h->stream));
+    return SJBG_OK;
+}
+
+int sjbg_kernel_stats(sjbg_handle *h, uint32_t index, char *name, size_t name_len, uint64_t *launches,
+                      double *total_ms) {
+    if (!h) return SJBG_E_INVALID;
+    if (index >= h->knames.size()) return SJBG_E_INVALID;
+    if (name && name_len) {
+        std::strncpy(name, h->knames[index].c_str(), name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    if (launches) *launches = h->klaunches[index];
+    if (total_ms) *total_ms = h->kms[index];
+    return SJBG_OK;
+}
+
+int sjbg_kernel_stats_reset(sjbg_handle *h) {
+    if (!h) return SJBG_E_INVALID;
+    std::fill(h->klaunches.begin(), h->klaunches.end(), 0);
+    std::fill(h->kms.begin(), h->kms.end(), 0.0);
+    return SJBG_OK;
+}
+
+uint64_t sjbg_launch_count(const sjbg_handle *h) { return h ? h->launches : 0; }
+
+}  // extern "C"

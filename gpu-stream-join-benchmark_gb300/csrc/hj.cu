@@ -1,0 +1,674 @@
+// hj.cu - lazy hash join (sm_103a).
+//
+// Replaces the reference's lazy GPU hash-join family
+// (src/sjb/windowing/lazy/executor/GPU/GPU_HJ.cu:9-309 and its NoOutput /
+// CountKernel / EstimatedSelectivity / Atomic variants), whose matching rule
+// is the lazy CPU_HJ's (src/sjb/windowing/lazy/executor/CPU/CPU_HJ.cpp:30-136):
+// every left tuple joins every right tuple of the window with an equal key.
+//
+// Design (many windows per call, four launches in total):
+//   1. part_hist     per 4096-tuple tile: bucket of each tuple -> shared histogram
+//                    -> one atomicAdd per non-empty bucket into the global counts.
+//   2. part_scan     exclusive scan of the counts of both sides -> bucket starts.
+//   3. part_scatter  per tile: local counting sort by bucket in shared memory,
+//                    one atomicAdd per bucket to reserve a range, then the tile
+//                    is written as contiguous per-bucket runs of (key,val) words.
+//   4. bucket_join   one CTA per (window, bucket): build an open-addressing table
+//                    in shared memory from the left run, probe with the right run.
+//        count mode: table slot = {key, count, sum fr(val)}; duplicates inside a
+//                    warp are pre-aggregated with __match_any_sync so a hot key
+//                    costs one shared atomic per warp; keys that do not fit go
+//                    back into the left run (compacted in place) and are joined
+//                    in a further pass, so any bucket, however skewed, finishes.
+//        enum mode:  table slot = {key, chain head}, chains over a staged chunk
+//                    of left vals; every pair is visited for the xor checksum
+//                    and, when asked, written with one atomic per warp.
+// The bucket of a key is its low radix bits (plain radix partitioning) or the
+// learned partitioner's prediction (learned.cu).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "learned.cuh"
+#include "runtime.h"
+
+namespace sjbg {
+
+constexpr int kTile = 4096;          // tuples per partitioning tile
+constexpr int kPartThreads = 512;
+constexpr int kJoinThreads = 512;
+constexpr uint32_t kMaxBucketsLog2 = 14;
+
+__device__ __forceinline__ uint32_t find_window(const uint32_t *prefix, uint32_t n, uint32_t t) {
+    // largest w with prefix[w] <= t  (prefix has n+1 entries, prefix[0] = 0)
+    uint32_t lo = 0, hi = n;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= t) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Partitioning model of the CTA's window: learned (when it has a model that
+// did not fall back) or plain radix on the key's low bits.
+struct Classifier {
+    const LearnedModel *m;   // null: radix
+    uint32_t mask;
+    __device__ __forceinline__ uint32_t bucket(uint32_t key) const {
+        return m ? learned_bucket(*m, key) : (key & mask);
+    }
+};
+
+__device__ __forceinline__ Classifier make_classifier(const WinPlan &wp, const LearnedModel *models) {
+    Classifier c;
+    c.m = nullptr;
+    if (wp.model != 0xFFFFFFFFu && !models[wp.model].fallback) c.m = &models[wp.model];
+    c.mask = (1u << wp.log2_buckets) - 1u;
+    return c;
+}
+
+// Lanes of a warp holding the same tag are combined: the group leader gets
+// the group size and the sum of the members' f.  All 32 lanes must call it.
+__device__ __forceinline__ bool warp_group(bool valid, uint32_t tag, unsigned long long f, bool want_sum,
+                                           uint32_t *gsize, unsigned long long *gsum) {
+    const unsigned full = 0xFFFFFFFFu;
+    const uint32_t lane = lane_id();
+    const unsigned active = __ballot_sync(full, valid);
+    unsigned grp = __match_any_sync(full, tag) & active;
+    if (!valid) grp = 1u << lane;
+    const int leader = __ffs(grp) - 1;
+    *gsize = __popc(grp);
+    *gsum = f;
+    if (want_sum) {
+        unsigned multi = __ballot_sync(full, valid && *gsize > 1 && (int)lane == leader);
+        while (multi) {
+            const int ld = __ffs(multi) - 1;
+            multi &= multi - 1;
+            const unsigned m = __shfl_sync(full, grp, ld);
+            const unsigned long long sm = warp_sum_u64(((m >> lane) & 1u) ? f : 0ull);
+            if ((int)lane == ld) *gsum = sm;
+        }
+    }
+    return valid && (int)lane == leader;
+}
+
+// ------------------------------------------------------------------ 1. histogram
+// Also aggregates heavy keys of learned windows: per heavy key, count and
+// sum of fr (left) / gs (right); heavy tuples are not partitioned.
+__global__ void __launch_bounds__(kPartThreads)
+part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
+                 uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                 uint32_t *__restrict__ cnt, uint32_t B, const LearnedModel *__restrict__ models,
+                 HeavyAcc *__restrict__ hacc) {
+    extern __shared__ uint32_t hist[];
+    __shared__ HeavySet hs;
+    __shared__ uint32_t hcnt[kMaxHeavy];
+    __shared__ unsigned long long hsum[kMaxHeavy];
+    const uint32_t tilesL = tileL[nwin];
+    const bool right = blockIdx.x >= tilesL;
+    const uint32_t t = right ? blockIdx.x - tilesL : blockIdx.x;
+    const uint32_t *tp = right ? tileR : tileL;
+    const uint32_t w = find_window(tp, nwin, t);
+    const WinPlan wp = wins[w];
+    const Classifier cls = make_classifier(wp, models);
+    const bool heavy = cls.m && cls.m->n_heavy;
+    const uint64_t nside = right ? wp.n_right : wp.n_left;
+    const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
+    const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+    const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
+    const uint32_t P = 1u << wp.log2_buckets;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
+    if (heavy) {
+        for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum[i] = 0; }
+        heavy_set_load(hs, cls.m);   // ends with a barrier
+    }
+    __syncthreads();
+    for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0, val = 0;
+        if (valid) {
+            const uint4 v = __ldg(src + i);   // whole 16-byte tuple, one vector load
+            key = v.x;
+            val = v.y;
+        }
+        uint32_t hid = kHeavyBucket;
+        if (heavy && valid) hid = heavy_find(hs, key);
+        uint32_t gs;
+        unsigned long long gsum;
+        if (heavy) {
+            const bool hv = valid && hid != kHeavyBucket;
+            const unsigned long long f = hv ? (right ? sjbg_gs(val) : sjbg_fr(val)) : 0ull;
+            if (warp_group(hv, hid, f, true, &gs, &gsum)) {
+                atomicAdd(&hcnt[hid], gs);
+                atomicAdd(&hsum[hid], gsum);
+            }
+        }
+        const bool light = valid && hid == kHeavyBucket;
+        const uint32_t b = light ? cls.bucket(key) : 0u;
+        if (warp_group(light, b, 0ull, false, &gs, &gsum)) atomicAdd(&hist[b], gs);
+    }
+    __syncthreads();
+    uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+        if (hist[i]) atomicAdd(&dst[i], hist[i]);
+    if (heavy) {
+        HeavyAcc *ha = hacc + (uint64_t)w * kMaxHeavy;
+        for (uint32_t i = threadIdx.x; i < cls.m->n_heavy; i += blockDim.x) {
+            if (!hcnt[i]) continue;
+            if (right) {
+                atomicAdd(&ha[i].cnt_r, (unsigned long long)hcnt[i]);
+                atomicAdd(&ha[i].sum_r, hsum[i]);
+            } else {
+                atomicAdd(&ha[i].cnt_l, (unsigned long long)hcnt[i]);
+                atomicAdd(&ha[i].sum_l, hsum[i]);
+            }
+        }
+    }
+}
+
+// Heavy keys' contribution per window: count += |L_k||R_k|, prod += (sum fr)(sum gs).
+__global__ void heavy_finish_kernel(const WinPlan *__restrict__ wins, uint32_t nwin,
+                                    const LearnedModel *__restrict__ models, const HeavyAcc *__restrict__ hacc,
+                                    WinAcc *__restrict__ acc) {
+    const uint32_t w = blockIdx.x;
+    const WinPlan wp = wins[w];
+    if (wp.model == 0xFFFFFFFFu || models[wp.model].fallback) return;
+    const uint32_t nh = models[wp.model].n_heavy;
+    unsigned long long c = 0, p = 0;
+    for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x) {
+        const HeavyAcc a = hacc[(uint64_t)w * kMaxHeavy + i];
+        c += a.cnt_l * a.cnt_r;
+        p += a.sum_l * a.sum_r;
+    }
+    flush_acc(&acc[w], c, 0, p);
+}
+
+// ------------------------------------------------------------------ 2. scan
+// Single-CTA exclusive scan of the bucket counts -> start and cursor.  The
+// left side (counts [0, B)) and the right side (counts [B, 2B)) are scanned
+// separately: each side's offsets index its own partitioned array.
+__global__ void __launch_bounds__(1024) part_scan_kernel(const uint32_t *__restrict__ cnt, uint32_t *__restrict__ start,
+                                                         uint32_t *__restrict__ cursor, uint32_t B) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t carry_s;
+    constexpr uint32_t kItems = 4;
+    const uint32_t chunk = blockDim.x * kItems;
+    for (uint32_t side = 0; side < 2; side++) {
+        const uint32_t lo = side * B, hi = lo + B;
+        if (threadIdx.x == 0) carry_s = 0;
+        __syncthreads();
+        for (uint32_t base = lo; base < hi; base += chunk) {
+            uint32_t v[kItems], s = 0;
+#pragma unroll
+            for (uint32_t k = 0; k < kItems; k++) {
+                const uint32_t i = base + threadIdx.x * kItems + k;
+                v[k] = i < hi ? cnt[i] : 0;
+                s += v[k];
+            }
+            uint32_t wt;
+            const uint32_t ex = warp_excl_scan(s, &wt);
+            if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
+            __syncthreads();
+            if (warp_id() == 0) {
+                const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0;
+                uint32_t tt;
+                warp_tot[lane_id()] = warp_excl_scan(x, &tt);
+            }
+            __syncthreads();
+            uint32_t run = carry_s + warp_tot[warp_id()] + ex;
+#pragma unroll
+            for (uint32_t k = 0; k < kItems; k++) {
+                const uint32_t i = base + threadIdx.x * kItems + k;
+                if (i < hi) {
+                    start[i] = run;
+                    cursor[i] = run;
+                }
+                run += v[k];
+            }
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) carry_s = run;
+            __syncthreads();
+        }
+    }
+}
+
+// Block-wide exclusive scan of P (<= 16384) shared counters in place.
+__device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
+    const uint32_t per = (P + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = min(P, threadIdx.x * per), b1 = min(P, b0 + per);
+    uint32_t s = 0;
+    for (uint32_t i = b0; i < b1; i++) s += a[i];
+    uint32_t tot;
+    uint32_t ex = warp_excl_scan(s, &tot);
+    if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
+    __syncthreads();
+    if (warp_id() == 0) {
+        uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0, tt;
+        warp_tot[lane_id()] = warp_excl_scan(x, &tt);
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[warp_id()] + ex;
+    for (uint32_t i = b0; i < b1; i++) {
+        uint32_t c = a[i];
+        a[i] = run;
+        run += c;
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------ 3. scatter
+__global__ void __launch_bounds__(kPartThreads)
+part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
+                    uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                    uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
+                    const LearnedModel *__restrict__ models) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ uint32_t warp_tot[32];
+    const uint32_t tilesL = tileL[nwin];
+    const bool right = blockIdx.x >= tilesL;
+    const uint32_t t = right ? blockIdx.x - tilesL : blockIdx.x;
+    const uint32_t *tp = right ? tileR : tileL;
+    const uint32_t w = find_window(tp, nwin, t);
+    const WinPlan wp = wins[w];
+    const uint64_t nside = right ? wp.n_right : wp.n_left;
+    const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
+    const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+    const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
+    const uint32_t P = 1u << wp.log2_buckets;
+
+    uint64_t *stage = reinterpret_cast<uint64_t *>(smem_raw);                  // kTile
+    uint16_t *sb = reinterpret_cast<uint16_t *>(stage + kTile);                // kTile bucket ids
+    uint32_t *lcnt = reinterpret_cast<uint32_t *>(sb + kTile);                 // P
+    uint32_t *gbase = lcnt + P;                                                // P
+    const Classifier cls = make_classifier(wp, models);
+    const bool heavy = cls.m && cls.m->n_heavy;
+    __shared__ HeavySet hs;
+    __shared__ uint32_t kept_s;
+
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) lcnt[i] = 0;
+    if (threadIdx.x == 0) kept_s = 0;
+    if (heavy) heavy_set_load(hs, cls.m);
+    __syncthreads();
+    constexpr int kPer = kTile / kPartThreads;
+    uint64_t e[kPer];
+    uint32_t bk[kPer], rk[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const uint32_t i = threadIdx.x + k * kPartThreads;
+        bk[k] = kHeavyBucket;
+        if (i < n) {
+            const uint4 v = __ldg(src + i);
+            e[k] = ((uint64_t)v.y << 32) | v.x;
+            if (!heavy || heavy_find(hs, v.x) == kHeavyBucket) {
+                bk[k] = cls.bucket(v.x);
+                rk[k] = atomicAdd(&lcnt[bk[k]], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    // reserve one global range per non-empty bucket
+    uint32_t *gcur = cursor + (right ? B : 0) + wp.bucket_base;
+    uint32_t kept = 0;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        const uint32_t c = lcnt[i];
+        gbase[i] = c ? atomicAdd(&gcur[i], c) : 0;
+        kept += c;
+    }
+    if (heavy) atomicAdd(&kept_s, kept);
+    block_scan_smem(lcnt, P, warp_tot);   // lcnt -> local offsets (ends with a barrier)
+    const uint32_t nk = heavy ? kept_s : n;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        if (bk[k] != kHeavyBucket) {
+            const uint32_t pos = lcnt[bk[k]] + rk[k];
+            stage[pos] = e[k];
+            sb[pos] = (uint16_t)bk[k];
+        }
+    }
+    __syncthreads();
+    uint64_t *out = right ? outR : outL;
+    for (uint32_t j = threadIdx.x; j < nk; j += blockDim.x) {
+        const uint32_t b = sb[j];
+        out[gbase[b] + (j - lcnt[b])] = stage[j];
+    }
+}
+
+// ------------------------------------------------------------------ 4. bucket join
+struct CountTable {
+    uint32_t *keys;              // C + 1 (slot C reserved for key 0xFFFFFFFF)
+    uint32_t *cnt;               // C + 1
+    unsigned long long *sumf;    // C + 1
+    uint32_t bits;
+    uint32_t limit;
+    uint32_t *occ;
+};
+
+// Insert `c` tuples of `key` with fr-sum `f`; false if the table is at its limit.
+__device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uint32_t c, unsigned long long f) {
+    const uint32_t C = 1u << t.bits;
+    if (key == kEmptyKey) {
+        atomicAdd(&t.cnt[C], c);
+        atomicAdd(&t.sumf[C], f);
+        return true;
+    }
+    uint32_t s = slot_hash(key, t.bits);
+    for (uint32_t probe = 0; probe < C; probe++) {
+        uint32_t k = *(volatile uint32_t *)&t.keys[s];
+        if (k == key) {
+            atomicAdd(&t.cnt[s], c);
+            atomicAdd(&t.sumf[s], f);
+            return true;
+        }
+        if (k == kEmptyKey) {
+            if (atomicAdd(t.occ, 1u) >= t.limit) {
+                atomicSub(t.occ, 1u);
+                return false;
+            }
+            uint32_t prev = atomicCAS(&t.keys[s], kEmptyKey, key);
+            if (prev == kEmptyKey || prev == key) {
+                if (prev == key) atomicSub(t.occ, 1u);
+                atomicAdd(&t.cnt[s], c);
+                atomicAdd(&t.sumf[s], f);
+                return true;
+            }
+            atomicSub(t.occ, 1u);
+        }
+        s = (s + 1) & (C - 1);
+    }
+    return false;
+}
+
+__device__ __forceinline__ int ct_lookup(const CountTable &t, uint32_t key) {
+    const uint32_t C = 1u << t.bits;
+    if (key == kEmptyKey) return t.cnt[C] ? (int)C : -1;
+    uint32_t s = slot_hash(key, t.bits);
+    for (uint32_t probe = 0; probe < C; probe++) {
+        uint32_t k = t.keys[s];
+        if (k == key) return (int)s;
+        if (k == kEmptyKey) return -1;
+        s = (s + 1) & (C - 1);
+    }
+    return -1;
+}
+
+// Warp-aggregated insert: lanes holding the same key combine (count, fr-sum)
+// and only the group leader touches the table.  All 32 lanes must call it.
+__device__ __forceinline__ bool agg_insert(const CountTable &t, bool valid, uint32_t key, unsigned long long f) {
+    uint32_t gsize;
+    unsigned long long gsum;
+    const bool lead = warp_group(valid, key, f, true, &gsize, &gsum);
+    bool ok = true;
+    if (lead) ok = ct_insert(t, key, gsize, gsum);
+    // every member follows its leader's outcome
+    const unsigned grp = __match_any_sync(0xFFFFFFFFu, key) & __ballot_sync(0xFFFFFFFFu, valid);
+    const int leader = valid ? __ffs(grp) - 1 : (int)lane_id();
+    return __shfl_sync(0xFFFFFFFFu, ok, leader);
+}
+
+__global__ void __launch_bounds__(kJoinThreads)
+bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
+                         const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
+                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t table_bits) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ uint32_t occ, novf;
+    const uint32_t b = blockIdx.x;
+    const uint32_t nR = cnt[b], nS = cnt[B + b];
+    if (nR == 0 || nS == 0) return;
+    uint64_t *Rb = partL + start[b];
+    const uint64_t *Sb = partR + start[B + b];
+    const uint32_t C = 1u << table_bits;
+    CountTable t;
+    t.sumf = reinterpret_cast<unsigned long long *>(smem_raw);
+    t.keys = reinterpret_cast<uint32_t *>(t.sumf + C + 1);
+    t.cnt = t.keys + C + 1;
+    t.bits = table_bits;
+    t.limit = C - C / 4;
+    t.occ = &occ;
+
+    unsigned long long count = 0, prod = 0;
+    uint32_t n = nR;
+    for (;;) {
+        for (uint32_t i = threadIdx.x; i <= C; i += blockDim.x) {
+            t.keys[i] = kEmptyKey;
+            t.cnt[i] = 0;
+            t.sumf[i] = 0;
+        }
+        if (threadIdx.x == 0) { occ = 0; novf = 0; }
+        __syncthreads();
+        for (uint32_t base = 0; base < n; base += blockDim.x) {
+            const uint32_t i = base + threadIdx.x;
+            const bool valid = i < n;
+            const uint64_t e = valid ? Rb[i] : 0;
+            __syncthreads();   // every read of this tile precedes any overflow write
+            const uint32_t key = (uint32_t)e;
+            const bool ok = agg_insert(t, valid, key, valid ? sjbg_fr((uint32_t)(e >> 32)) : 0ull);
+            if (valid && !ok) Rb[atomicAdd(&novf, 1u)] = e;
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < nS; j += blockDim.x) {
+            const uint64_t e = Sb[j];
+            const int s = ct_lookup(t, (uint32_t)e);
+            if (s >= 0) {
+                count += t.cnt[s];
+                prod += t.sumf[s] * sjbg_gs((uint32_t)(e >> 32));
+            }
+        }
+        __syncthreads();
+        n = novf;
+        __syncthreads();
+        if (n == 0) break;
+    }
+    flush_acc(&acc[bucket_win[b]], count, 0, prod);
+}
+
+constexpr uint32_t kEnumChunk = 4096;  // left tuples per chained chunk
+constexpr uint32_t kNil = 0xFFFFFFFFu;
+
+__global__ void __launch_bounds__(kJoinThreads)
+bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
+                        const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
+                        const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc,
+                        const WinPlan *__restrict__ wins, sjbg_pair *__restrict__ pairs, uint32_t table_bits) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    const uint32_t b = blockIdx.x;
+    const uint32_t nR = cnt[b], nS = cnt[B + b];
+    if (nR == 0 || nS == 0) return;
+    const uint64_t *Rb = partL + start[b];
+    const uint64_t *Sb = partR + start[B + b];
+    const uint32_t w = bucket_win[b];
+    const uint32_t C = 1u << table_bits;
+    uint32_t *keys = reinterpret_cast<uint32_t *>(smem_raw);   // C + 1
+    uint32_t *head = keys + C + 1;                             // C + 1
+    uint32_t *next = head + C + 1;                             // kEnumChunk
+    uint32_t *vals = next + kEnumChunk;                        // kEnumChunk
+    const uint64_t pcap = pairs ? wins[w].pairs_cap : 0;
+    sjbg_pair *pout = pairs ? pairs + wins[w].pairs_off : nullptr;
+
+    unsigned long long count = 0, prod = 0, xr = 0;
+    for (uint32_t c0 = 0; c0 < nR; c0 += kEnumChunk) {
+        const uint32_t m = min(kEnumChunk, nR - c0);
+        for (uint32_t i = threadIdx.x; i <= C; i += blockDim.x) {
+            keys[i] = kEmptyKey;
+            head[i] = kNil;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
+            const uint64_t e = Rb[c0 + i];
+            const uint32_t key = (uint32_t)e;
+            vals[i] = (uint32_t)(e >> 32);
+            uint32_t s;
+            if (key == kEmptyKey) {
+                s = C;
+            } else {
+                s = slot_hash(key, table_bits);
+                // at most m <= C/2 keys: a free or matching slot exists within C probes
+                for (uint32_t p = 0; p < C; p++) {
+                    const uint32_t prev = atomicCAS(&keys[s], kEmptyKey, key);
+                    if (prev == kEmptyKey || prev == key) break;
+                    s = (s + 1) & (C - 1);
+                }
+            }
+            next[i] = atomicExch(&head[s], i);
+        }
+        __syncthreads();
+        // probe: loop bound is uniform per warp so the pair reservation can use shuffles
+        for (uint32_t j0 = 0; j0 < nS; j0 += blockDim.x) {
+            const uint32_t j = j0 + threadIdx.x;
+            uint32_t h = kNil, sv = 0;
+            if (j < nS) {
+                const uint64_t e = Sb[j];
+                const uint32_t key = (uint32_t)e;
+                sv = (uint32_t)(e >> 32);
+                uint32_t s = kNil;
+                if (key == kEmptyKey) {
+                    s = C;
+                } else {
+                    uint32_t q = slot_hash(key, table_bits);
+                    for (uint32_t p = 0; p <= C; p++) {
+                        const uint32_t k = keys[q];
+                        if (k == key) { s = q; break; }
+                        if (k == kEmptyKey) break;
+                        q = (q + 1) & (C - 1);
+                    }
+                }
+                if (s != kNil) h = head[s];
+            }
+            uint32_t mine = 0;
+            const unsigned long long gs = sjbg_gs(sv);
+            for (uint32_t i = h; i != kNil; i = next[i]) {
+                const uint32_t rv = vals[i];
+                xr ^= sjbg_pair_hash(rv, sv);
+                prod += sjbg_fr(rv) * gs;
+                mine++;
+            }
+            count += mine;
+            if (pout) {
+                uint32_t tot;
+                const uint32_t ex = warp_excl_scan(mine, &tot);
+                unsigned long long base = 0;
+                if (lane_id() == 0 && tot) base = atomicAdd(&acc[w].npairs, (unsigned long long)tot);
+                base = __shfl_sync(0xFFFFFFFFu, base, 0) + ex;
+                for (uint32_t i = h; i != kNil; i = next[i]) {
+                    if (base < pcap) pout[base] = sjbg_pair{vals[i], sv};
+                    base++;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    flush_acc(&acc[w], count, xr, prod);
+}
+
+// ------------------------------------------------------------------ host driver
+static uint32_t ceil_log2(uint64_t x) {
+    uint32_t b = 0;
+    while (((uint64_t)1 << b) < x) b++;
+    return b;
+}
+
+int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                  sjbg_pair *dPairs, WinAcc *acc, bool enumerate, uint32_t *part_used) {
+    if (n == 0) return SJBG_OK;
+    const uint32_t part = h->cfg.partitioner;
+    const bool learned = part == SJBG_PART_LEARNED;
+    if (part_used) *part_used = learned ? SJBG_PART_LEARNED : SJBG_PART_RADIX;
+    const uint64_t target = enumerate ? 2048 : 4096;   // left tuples per bucket (autotuner may change)
+
+    // ---- plan
+    std::vector<WinPlan> plan(n);
+    std::vector<uint32_t> tileL(n + 1), tileR(n + 1);
+    uint64_t B = 0, totL = 0, totR = 0;
+    uint32_t maxP = 1;
+    for (uint32_t w = 0; w < n; w++) {
+        const WinHost &wh = wins[w];
+        WinPlan &p = plan[w];
+        p.left_off = wh.left_off; p.n_left = wh.n_left; p.right_off = wh.right_off; p.n_right = wh.n_right;
+        p.pairs_off = wh.pairs_off; p.pairs_cap = dPairs ? wh.pairs_cap : 0;
+        uint32_t lg;
+        if (learned) lg = learned_log2_buckets(h, wh.n_left);
+        else if (h->cfg.radix_bits) lg = h->cfg.radix_bits;
+        else lg = ceil_log2((wh.n_left + target - 1) / target);
+        lg = std::min(lg, kMaxBucketsLog2);
+        if (wh.n_left == 0 || wh.n_right == 0) lg = 0;
+        p.log2_buckets = lg;
+        p.bucket_base = (uint32_t)B;
+        p.model = 0xFFFFFFFFu;
+        B += 1ull << lg;
+        maxP = std::max(maxP, 1u << lg);
+        tileL[w + 1] = tileL[w] + (uint32_t)((wh.n_left + kTile - 1) / kTile);
+        tileR[w + 1] = tileR[w] + (uint32_t)((wh.n_right + kTile - 1) / kTile);
+        totL += wh.n_left;
+        totR += wh.n_right;
+    }
+    if (B > 0xFFFFFFFFull / 4 || totL >= 0xFFFFFFFFull || totR >= 0xFFFFFFFFull)
+        return fail(h, SJBG_E_CAPACITY, "hash join batch exceeds 2^32 tuples per side");
+    std::vector<uint32_t> bwin(B);
+    for (uint32_t w = 0; w < n; w++)
+        for (uint32_t k = 0; k < (1u << plan[w].log2_buckets); k++) bwin[plan[w].bucket_base + k] = w;
+
+    // ---- upload plan, tile prefixes and bucket->window map in one copy
+    const size_t planB = sizeof(WinPlan) * n, tileB = sizeof(uint32_t) * (n + 1), bwB = sizeof(uint32_t) * B;
+    const size_t upB = planB + 2 * tileB + bwB;
+    uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 0, upB));
+    uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_WIN_PLAN, upB));
+    if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "plan buffers");
+    std::memcpy(hst, plan.data(), planB);
+    std::memcpy(hst + planB, tileL.data(), tileB);
+    std::memcpy(hst + planB + tileB, tileR.data(), tileB);
+    std::memcpy(hst + planB + 2 * tileB, bwin.data(), bwB);
+    SJBG_CK(h, cudaMemcpyAsync(dev, hst, upB, cudaMemcpyHostToDevice, h->stream));
+    WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
+    const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
+    const uint32_t *dTileR = reinterpret_cast<const uint32_t *>(dev + planB + tileB);
+    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 2 * tileB);
+
+    uint32_t *dCnt = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CNT, sizeof(uint32_t) * 2 * B));
+    uint32_t *dStart = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_START, sizeof(uint32_t) * 2 * B));
+    uint32_t *dCur = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CURSOR, sizeof(uint32_t) * 2 * B));
+    uint64_t *dPL = static_cast<uint64_t *>(ws_get(h, WS_PART_LEFT, sizeof(uint64_t) * std::max<uint64_t>(totL, 1)));
+    uint64_t *dPR = static_cast<uint64_t *>(ws_get(h, WS_PART_RIGHT, sizeof(uint64_t) * std::max<uint64_t>(totR, 1)));
+    if (!dCnt || !dStart || !dCur || !dPL || !dPR) return fail(h, SJBG_E_NOMEM, "partition buffers");
+
+    const LearnedModel *dModels = nullptr;
+    HeavyAcc *dHeavy = nullptr;
+    if (learned) {
+        int rc = learned_prepare(h, dL, dR, plan.data(), n, dPlan, &dModels, !enumerate);
+        if (rc) return rc;
+        dHeavy = static_cast<HeavyAcc *>(ws_get(h, WS_HEAVY, sizeof(HeavyAcc) * kMaxHeavy * n));
+        if (!dHeavy) return fail(h, SJBG_E_NOMEM, "heavy-key accumulators");
+        SJBG_CK(h, cudaMemsetAsync(dHeavy, 0, sizeof(HeavyAcc) * kMaxHeavy * n, h->stream));
+    }
+
+    SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
+    const uint32_t tiles = tileL[n] + tileR[n];
+    if (tiles) {
+        SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(tiles), dim3(kPartThreads), sizeof(uint32_t) * maxP,
+                          dL, dR, dPlan, n, dTileL, dTileR, dCnt, (uint32_t)B, dModels, dHeavy));
+        if (learned)
+            SJBG_CK(h, launch(h, "heavy_finish", heavy_finish_kernel, dim3(n), dim3(256), 0, (const WinPlan *)dPlan, n,
+                              dModels, (const HeavyAcc *)dHeavy, acc));
+        SJBG_CK(h, launch(h, "part_scan", part_scan_kernel, dim3(1), dim3(1024), 0, dCnt, dStart, dCur,
+                          (uint32_t)B));
+        const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;
+        allow_big_smem(part_scatter_kernel, scatterSmem);
+        SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(tiles), dim3(kPartThreads), scatterSmem,
+                          dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels));
+    }
+    if (enumerate) {
+        const uint32_t bits = 13;   // 8192 slots for chunks of 4096
+        const size_t smem = sizeof(uint32_t) * (2 * ((1u << bits) + 1) + 2 * kEnumChunk);
+        allow_big_smem(bucket_join_enum_kernel, smem);
+        SJBG_CK(h, launch(h, "bucket_join_enum", bucket_join_enum_kernel, dim3((uint32_t)B), dim3(kJoinThreads), smem,
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits));
+    } else {
+        const uint32_t bits = 13;
+        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
+        allow_big_smem(bucket_join_count_kernel, smem);
+        SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, dim3((uint32_t)B), dim3(kJoinThreads), smem,
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, bits));
+    }
+    return SJBG_OK;
+}
+
+}  // namespace sjbg

@@ -1,0 +1,106 @@
+// learned.cuh - learned key-CDF partitioner: model layout and device-side inference.
+//
+// No reference counterpart.  A window's model is a monotone two-stage
+// piecewise-linear approximation of the CDF of its light (non-heavy) keys:
+//   x      = clamp((key - kmin) * inv_range, 0, 1)                (FP32)
+//   leaf   = clamp(floor((root_a * x + root_b) * leaves), 0, leaves-1)
+//   cdf    = clamp(mean_y[leaf] + slope[leaf] * (x - mean_x[leaf]), lo[leaf], hi[leaf])
+//   bucket = min(P - 1, floor(cdf * P))
+// lo/hi are the smallest/largest sampled CDF values routed to the leaf, made
+// non-decreasing across leaves, which keeps the whole map monotone in key.
+// Heavy keys (sampled frequency above one bucket's fair share) are not
+// partitioned at all: their per-window count and checksum sums are
+// aggregated while partitioning and combined as |L_k|*|R_k| at the end.
+#pragma once
+
+#include "common.cuh"
+
+namespace sjbg {
+
+constexpr uint32_t kMaxLeaves = 256;
+constexpr uint32_t kMaxHeavy = 256;
+constexpr uint32_t kHeavySlots = 512;          // shared-memory heavy-key table
+constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu; // classify(): heavy key marker
+
+struct LearnedModel {
+    float kmin, inv_range, root_a, root_b;
+    uint32_t leaves, log2_buckets, fallback, n_heavy;
+    float slope[kMaxLeaves], mean_x[kMaxLeaves], mean_y[kMaxLeaves], lo[kMaxLeaves], hi[kMaxLeaves];
+    uint32_t heavy_keys[kMaxHeavy];
+};
+
+// Per-window, per-heavy-key aggregates.
+struct HeavyAcc {
+    unsigned long long cnt_l, sum_l, cnt_r, sum_r;
+};
+
+__device__ __forceinline__ uint32_t learned_bucket(const LearnedModel &m, uint32_t key) {
+    const uint32_t P = 1u << m.log2_buckets;
+    float x = ((float)key - m.kmin) * m.inv_range;
+    x = fminf(fmaxf(x, 0.0f), 1.0f);
+    int leaf = (int)floorf((m.root_a * x + m.root_b) * (float)m.leaves);
+    leaf = min(max(leaf, 0), (int)m.leaves - 1);
+    float y = m.mean_y[leaf] + m.slope[leaf] * (x - m.mean_x[leaf]);
+    y = fminf(fmaxf(y, m.lo[leaf]), m.hi[leaf]);
+    uint32_t b = (uint32_t)(y * (float)P);
+    return b < P ? b : P - 1;
+}
+
+// Shared-memory heavy-key set: slot -> (key, index); empty slots hold kEmptyKey
+// in the key and 0xFFFFFFFF in the index (the index distinguishes a heavy key
+// equal to 0xFFFFFFFF from an empty slot).
+struct HeavySet {
+    uint32_t keys[kHeavySlots];
+    uint32_t idx[kHeavySlots];
+};
+
+__device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, 9); }
+
+// Cooperative load of a model's heavy keys (all threads; ends with a barrier).
+__device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel *m) {
+    for (uint32_t i = threadIdx.x; i < kHeavySlots; i += blockDim.x) {
+        hs.keys[i] = kEmptyKey;
+        hs.idx[i] = 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    if (m && !m->fallback) {
+        for (uint32_t h = threadIdx.x; h < m->n_heavy; h += blockDim.x) {
+            uint32_t key = m->heavy_keys[h];
+            uint32_t s = heavy_slot(key);
+            for (uint32_t p = 0; p < kHeavySlots; p++) {
+                // claim by index, which is unique per heavy key
+                if (atomicCAS(&hs.idx[s], 0xFFFFFFFFu, h) == 0xFFFFFFFFu) {
+                    hs.keys[s] = key;
+                    break;
+                }
+                s = (s + 1) & (kHeavySlots - 1);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Index of `key` among the heavy keys, or kHeavyBucket when it is light.
+__device__ __forceinline__ uint32_t heavy_find(const HeavySet &hs, uint32_t key) {
+    uint32_t s = heavy_slot(key);
+    for (uint32_t p = 0; p < kHeavySlots; p++) {
+        uint32_t id = hs.idx[s];
+        if (id == 0xFFFFFFFFu) return kHeavyBucket;
+        if (hs.keys[s] == key) return id;
+        s = (s + 1) & (kHeavySlots - 1);
+    }
+    return kHeavyBucket;
+}
+
+}  // namespace sjbg
+
+struct sjbg_handle;
+namespace sjbg {
+struct WinPlan;
+uint32_t learned_log2_buckets(sjbg_handle *h, uint64_t n_left);
+// Sample, fit and check every window's model; writes models and sets
+// WinPlan::model on device (dPlan) for the windows that keep their model.
+// allow_heavy = false keeps every key in the partitions (needed when pairs are enumerated).
+int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinPlan *plan, uint32_t n,
+                    WinPlan *dPlan, const LearnedModel **dModels, bool allow_heavy);
+}  // namespace sjbg

@@ -1,0 +1,171 @@
+"""GPU parity tests of the lazy hash join (through the C ABI) against the
+oracle and the golden fixtures made by the reference's CPU joiners."""
+import numpy as np
+import pytest
+
+from helpers import load_fixture, make_tuples, sorted_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def windows_of(n_windows, W):
+    return [(w * W, W, w * W, W, w * W * 4, W * 4) for w in range(n_windows)]
+
+
+@pytest.mark.parametrize("part", ["radix", "learned"])
+def test_golden_uniform_windows_with_pairs(lib, golden, part):
+    fx, meta = load_fixture("lazy_uniform_small"), golden["lazy_uniform_small"]
+    W = meta["W"]
+    nwin = len(meta["windows"])
+    pairs = np.zeros(nwin * W * 4, lib.PAIR_DTYPE)
+    p = lib.PART_RADIX if part == "radix" else lib.PART_LEARNED
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_ATOMIC, partitioner=p, max_tuples_per_window=W) as j:
+        res = j.lazy_execute_batch(fx["left"], fx["right"], windows_of(nwin, W), pairs=pairs)
+    for w, (r, win) in enumerate(zip(res, meta["windows"])):
+        assert r["count"] == win["count"] == win["ref_hj"]
+        assert r["xor"] == win["xor"] and r["prod"] == win["prod"]
+        got = pairs[w * W * 4: w * W * 4 + r["n_pairs"]]
+        if f"pairs_w{w}" in fx:
+            assert np.array_equal(sorted_pairs(got), sorted_pairs(fx[f"pairs_w{w}"]))
+
+
+def test_config_uniform_16x65536(lib, oracle):
+    """The 16 x 65,536 uniform workload: count, xor and prod per window."""
+    W, n = 65536, 16
+    left = oracle.gen_uniform(0, n * W, 1, 65536)
+    right = oracle.gen_uniform(0, n * W, 2, 65536)
+    descs = [(w * W, W, w * W, W, 0, 0) for w in range(n)]
+    want, _ = oracle.join_windows(left, right, descs, enumerate_pairs=True)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_NO_OUTPUT, flags=lib.F_XOR, max_tuples_per_window=W) as j:
+        got = j.lazy_execute_batch(left, right, descs)
+    for g, w in zip(got, want):
+        assert (g["count"], g["xor"], g["prod"]) == (w["count"], w["xor"], w["prod"])
+    # the reference's own count for one window (restated CPU_HJ)
+    assert got[0]["count"] == oracle.lazy_hj_count(left[:W], right[:W], 65536, 8192, 4)
+
+
+@pytest.mark.parametrize("z", [0.5, 1.0, 1.5])
+@pytest.mark.parametrize("part", ["radix", "learned"])
+def test_golden_zipf_counts(lib, golden, z, part):
+    tag = f"zipf_small_z{str(z).replace('.', 'p')}"
+    fx, meta = load_fixture(tag), golden[tag]
+    W = meta["W"]
+    p = lib.PART_RADIX if part == "radix" else lib.PART_LEARNED
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=p, max_tuples_per_window=W) as j:
+        res = j.lazy_execute_batch(fx["left"], fx["right"], [(w * W, W, w * W, W) for w in range(2)])
+    for r, win in zip(res, meta["windows"]):
+        assert r["count"] == win["count"] == win["ref_smj"]
+        assert r["prod"] == win["prod"]
+
+
+def test_golden_batched_uneven_windows(lib, golden):
+    fx, meta = load_fixture("batched_small"), golden["batched_small"]
+    descs, off = [], 0
+    for n in meta["sizes"]:
+        descs.append((off, n, off, n))
+        off += n
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, flags=lib.F_XOR, max_tuples_per_window=1 << 12) as j:
+        res = j.lazy_execute_batch(fx["left"], fx["right"], descs)
+    for r, win in zip(res, meta["windows"]):
+        assert (r["count"], r["xor"], r["prod"]) == (win["count"], win["xor"], win["prod"])
+
+
+@pytest.mark.parametrize("part", ["radix", "learned"])
+def test_edge_cases(lib, oracle, part):
+    p = lib.PART_RADIX if part == "radix" else lib.PART_LEARNED
+    cases = [
+        ([], []), ([1, 2, 3], []), ([], [4]), ([5], [5]),
+        ([7] * 3000, [7] * 2000),                                  # one hot key
+        ([0xFFFFFFFF, 0, 0xFFFFFFFF, 9], [0xFFFFFFFF, 9, 9]),      # the all-ones key
+        (list(range(10000)), list(range(5000, 15000))),            # half overlap
+        ([3] * 5000 + list(range(100, 9000)), [3] * 3000 + list(range(50, 7000))),  # hot key + tail
+    ]
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_ATOMIC, partitioner=p, max_tuples_per_window=1 << 16) as j:
+        for kl, kr in cases:
+            l, r = make_tuples(kl), make_tuples(kr, first=len(kl))
+            want = oracle.join(l, r, enumerate_pairs=True, pairs_capacity=1 << 24)
+            pairs = np.zeros(max(want["count"], 1), lib.PAIR_DTYPE)
+            got = j.lazy_execute(l, r, pairs=pairs)
+            assert got["count"] == want["count"], (kl[:5], kr[:5])
+            assert got["xor"] == want["xor"] and got["prod"] == want["prod"]
+            assert np.array_equal(sorted_pairs(pairs[:got["n_pairs"]]), sorted_pairs(want["pairs"]))
+
+
+def test_skewed_count_mode_overflow_passes(lib, oracle):
+    """Buckets with more distinct keys than a shared table holds are joined in several passes."""
+    n = 1 << 18
+    rng = np.random.default_rng(1)
+    l = make_tuples(rng.integers(0, 1 << 30, n))
+    r = make_tuples(np.concatenate([l["key"][: n // 2], rng.integers(0, 1 << 30, n // 2)]), first=n)
+    want = oracle.join(l, r, enumerate_pairs=False)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, radix_bits=2, max_tuples_per_window=n) as j:
+        got = j.lazy_execute(l, r)
+    assert (got["count"], got["prod"]) == (want["count"], want["prod"])
+
+
+def test_pairs_truncation_and_count_kernel(lib, oracle):
+    l, r = make_tuples([1] * 100), make_tuples([1] * 100)
+    small = np.zeros(50, lib.PAIR_DTYPE)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_ATOMIC, max_tuples_per_window=1024) as j:
+        got = j.lazy_execute(l, r, pairs=small)
+    assert got["count"] == 10000 and got["n_pairs"] == 50 and got["flags"] & lib.WR_PAIRS_TRUNCATED
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_COUNT_KERNEL, max_tuples_per_window=1024) as j:
+        with pytest.raises(lib.SjbgError) as e:
+            j.lazy_execute(l, r, pairs=small)
+        assert e.value.code == 5
+
+
+def test_capacity_is_enforced(lib):
+    l = make_tuples(range(100))
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, max_tuples_per_window=64) as j:
+        with pytest.raises(lib.SjbgError) as e:
+            j.lazy_execute(l, l)
+        assert e.value.code == 5
+
+
+def test_device_inputs_and_ring_api(lib, oracle):
+    torch = pytest.importorskip("torch")
+    W = 1 << 14
+    left = oracle.gen_uniform(0, W, 1, W)
+    right = oracle.gen_uniform(0, W, 2, W)
+    want = oracle.join(left, right, enumerate_pairs=False)
+    dl = torch.from_numpy(left.view(np.uint8)).cuda()
+    dr = torch.from_numpy(right.view(np.uint8)).cuda()
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, max_tuples_per_window=W, batch_size=1024) as j:
+        got = j.lazy_execute(dl, dr, mem=lib.MEM_DEVICE, n_left=W, n_right=W)
+        assert (got["count"], got["prod"]) == (want["count"], want["prod"])
+        # reference-style ring: batches of 1024 at scattered ring offsets
+        ring_l = np.zeros(4 * W, lib.TUPLE_DTYPE)
+        ring_r = np.zeros(4 * W, lib.TUPLE_DTYPE)
+        offs = [(3 * i + 1) * 1024 for i in range(W // 1024)]
+        for i, o in enumerate(offs):
+            ring_l[o:o + 1024] = left[i * 1024:(i + 1) * 1024]
+            ring_r[o:o + 1024] = right[i * 1024:(i + 1) * 1024]
+        got2 = j.lazy_execute_ring(ring_l, offs, ring_r, offs)
+        assert (got2["count"], got2["prod"]) == (want["count"], want["prod"])
+
+
+def test_device_generator_matches_host(lib, oracle):
+    torch = pytest.importorskip("torch")
+    n, D = 100000, 1 << 16
+    buf = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    T = oracle.zipf_table(D, 1.2)
+    dT = torch.from_numpy(T.view(np.int64)).cuda()
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY) as j:
+        j.generate(buf.data_ptr(), 12345, n, 1, D)
+        got = buf.cpu().numpy().view(lib.TUPLE_DTYPE)
+        assert np.array_equal(got, oracle.gen_uniform(12345, n, 1, D))
+        j.generate(buf.data_ptr(), 7, n, 2, D, dT.data_ptr(), 3)
+        got = buf.cpu().numpy().view(lib.TUPLE_DTYPE)
+        assert np.array_equal(got, oracle.gen_zipf(7, n, 2, T, D, 3))
+
+
+def test_profile_counts_kernels(lib, oracle):
+    W = 4096
+    left = oracle.gen_uniform(0, W, 1, W)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, flags=lib.F_PROFILE, max_tuples_per_window=W) as j:
+        j.lazy_execute(left, left)
+        st = j.kernel_stats()
+        assert {"part_hist", "part_scan", "part_scatter", "bucket_join_count"} <= set(st)
+        assert all(v[0] >= 1 and v[1] > 0 for v in st.values())
+        assert j.launch_count() >= 4
