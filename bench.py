@@ -42,6 +42,8 @@ WORKLOADS = {
     "skewed_hj_z1.0": (8, 1 << 24, 1 << 24, 1.0),
     "skewed_hj_z0.5": (8, 1 << 24, 1 << 24, 0.5),
     "uniform_hj_16x65536": (16, 65536, 65536, None),
+    # reduced case of the skewed workload for profiler captures (inputs still > L2)
+    "skewed_hj_small": (2, 1 << 22, 1 << 24, 1.5),
 }
 
 
@@ -189,8 +191,10 @@ def main():
         T = O.zipf_table(D, z)
         dT = torch.from_numpy(T.view(np.int64)).cuda()
         table_ptr = dT.data_ptr()
-    flags_common = dict(algorithm=sjbg.ALG_HJ, progressiveness=sjbg.LAZY, max_tuples_per_window=W, device=local,
-                        radix_bits=10 if W >= (1 << 20) else 0)
+    flags_common = dict(algorithm=sjbg.ALG_HJ, progressiveness=sjbg.LAZY, max_tuples_per_window=W, device=local)
+    # plain radix: the specified fan-out 2^10 for the 2^24 windows; the learned
+    # partitioner sizes its own fan-out (about 4096 left tuples per bucket)
+    plain_bits = 10 if W >= (1 << 20) else 0
     gen = sjbg.Joiner(**flags_common)
     # each rank joins its own windows (weak scaling: windows are independent)
     first = rank * total
@@ -202,9 +206,10 @@ def main():
     windows = [(w * W, W, w * W, W, 0, 0) for w in range(nwin)]
     descs = (sjbg.WindowDesc * nwin)(*[sjbg.WindowDesc(*d) for d in windows])
     learned = sjbg.Joiner(partitioner=sjbg.PART_LEARNED, **flags_common)
-    plain = sjbg.Joiner(partitioner=sjbg.PART_RADIX, **flags_common)
+    plain = sjbg.Joiner(partitioner=sjbg.PART_RADIX, radix_bits=plain_bits, **flags_common)
+    radix_auto = sjbg.Joiner(partitioner=sjbg.PART_RADIX, **flags_common)
     stream = torch.cuda.Stream()
-    for j in (learned, plain):
+    for j in (learned, plain, radix_auto):
         j.set_stream(stream.cuda_stream)
 
     def run_steps(j, k, res):
@@ -234,7 +239,9 @@ def main():
         ms_learned, res_learned = timed(learned, args.steps)
     launches = (learned.launch_count() - launches0) * args.steps // (args.steps + args.warmup)
     ms_plain, res_plain = timed(plain, args.steps)
-    same = [(a[0], a[1]) for a in res_learned] == [(b[0], b[1]) for b in res_plain]
+    ms_radix_auto, res_radix_auto = timed(radix_auto, args.steps)
+    same = ([(a[0], a[1]) for a in res_learned] == [(b[0], b[1]) for b in res_plain]
+            == [(b[0], b[1]) for b in res_radix_auto])
 
     # ---- per-window latency (single-window calls, device time per call)
     lat = []
@@ -291,10 +298,13 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": args.workload, "windows": nwin, "tuples_per_window_per_stream": W,
                    "key_domain": D, "zipf_z": z, "partitioner": "learned (256 leaves, 1% sample)",
-                   "fanout": 1 << flags_common["radix_bits"] if flags_common["radix_bits"] else "auto",
+                   "learned_fanout": "auto (about 4096 left tuples per bucket)",
                    "l2": "inputs larger than L2 (4 GiB per step)" if total * 32 > (256 << 20) else "L2-resident"},
-        "plain": {"value": tuples / (ms_plain * 1e-3), "ms_per_step": ms_plain, "partitioner": "radix 2^10"},
+        "plain": {"value": tuples / (ms_plain * 1e-3), "ms_per_step": ms_plain,
+                  "partitioner": f"radix 2^{plain_bits}" if plain_bits else "radix, auto fan-out"},
+        "radix_same_fanout_as_learned": {"value": tuples / (ms_radix_auto * 1e-3), "ms_per_step": ms_radix_auto},
         "learned_over_plain": ms_plain / ms_learned,
+        "learned_windows": sum(1 for a in res_learned if a[2] == sjbg.PART_LEARNED),
         "outputs_identical_learned_vs_plain": same,
         "latency": {"p50_ms": p50, "p99_ms": p99, "windows": len(lat), "unit": "ms per window call"},
         "e2e": {"value": tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": 32 * total,
@@ -314,6 +324,7 @@ def main():
         print(json.dumps(out))
     learned.close()
     plain.close()
+    radix_auto.close()
 
 
 if __name__ == "__main__":

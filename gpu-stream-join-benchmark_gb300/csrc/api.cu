@@ -154,6 +154,10 @@ static void fill_result(const sjbg_handle *h, const WinAcc &a, const WinHost &w,
     out->count = a.count;
     out->prod_checksum = a.prod;
     out->partitioner_used = part_used;
+    if (part_used == SJBG_PART_LEARNED && (a.info & kInfoFallback)) {
+        out->partitioner_used = SJBG_PART_RADIX;
+        out->flags |= SJBG_WR_FALLBACK;
+    }
     out->ms = ms;
     if (enumerate) {
         out->xor_checksum = a.xr;

@@ -26,7 +26,10 @@ struct WinAcc {
     unsigned long long xr;
     unsigned long long prod;
     unsigned long long npairs;   // pairs produced (may exceed capacity)
+    unsigned long long info;     // kInfo* bits | heavy keys << 32 (learned partitioning)
 };
+
+enum : unsigned long long { kInfoLearned = 1ull, kInfoFallback = 2ull };
 
 // Per-window plan entry of a lazy batch, in device memory.
 struct WinPlan {

@@ -173,8 +173,13 @@ __global__ void heavy_finish_kernel(const WinPlan *__restrict__ wins, uint32_t n
                                     WinAcc *__restrict__ acc) {
     const uint32_t w = blockIdx.x;
     const WinPlan wp = wins[w];
-    if (wp.model == 0xFFFFFFFFu || models[wp.model].fallback) return;
+    if (wp.model == 0xFFFFFFFFu) return;
+    if (models[wp.model].fallback) {
+        if (threadIdx.x == 0) acc[w].info = kInfoFallback;
+        return;
+    }
     const uint32_t nh = models[wp.model].n_heavy;
+    if (threadIdx.x == 0) acc[w].info = kInfoLearned | ((unsigned long long)nh << 32);
     unsigned long long c = 0, p = 0;
     for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x) {
         const HeavyAcc a = hacc[(uint64_t)w * kMaxHeavy + i];
@@ -335,16 +340,18 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
 }
 
 // ------------------------------------------------------------------ 4. bucket join
+constexpr uint32_t kMaxProbe = 64;   // linear-probe bound of the count tables
+
 struct CountTable {
     uint32_t *keys;              // C + 1 (slot C reserved for key 0xFFFFFFFF)
     uint32_t *cnt;               // C + 1
     unsigned long long *sumf;    // C + 1
     uint32_t bits;
-    uint32_t limit;
-    uint32_t *occ;
 };
 
-// Insert `c` tuples of `key` with fr-sum `f`; false if the table is at its limit.
+// Insert `c` tuples of `key` with fr-sum `f`.  A key that finds neither itself
+// nor a free slot within kMaxProbe slots is refused (false) and joined in a
+// later pass; lookups use the same bound, so a refused key is never half-found.
 __device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uint32_t c, unsigned long long f) {
     const uint32_t C = 1u << t.bits;
     if (key == kEmptyKey) {
@@ -353,26 +360,16 @@ __device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uin
         return true;
     }
     uint32_t s = slot_hash(key, t.bits);
-    for (uint32_t probe = 0; probe < C; probe++) {
+    for (uint32_t probe = 0; probe < kMaxProbe; probe++) {
         uint32_t k = *(volatile uint32_t *)&t.keys[s];
+        if (k == kEmptyKey) {
+            const uint32_t prev = atomicCAS(&t.keys[s], kEmptyKey, key);
+            k = prev == kEmptyKey ? key : prev;
+        }
         if (k == key) {
             atomicAdd(&t.cnt[s], c);
             atomicAdd(&t.sumf[s], f);
             return true;
-        }
-        if (k == kEmptyKey) {
-            if (atomicAdd(t.occ, 1u) >= t.limit) {
-                atomicSub(t.occ, 1u);
-                return false;
-            }
-            uint32_t prev = atomicCAS(&t.keys[s], kEmptyKey, key);
-            if (prev == kEmptyKey || prev == key) {
-                if (prev == key) atomicSub(t.occ, 1u);
-                atomicAdd(&t.cnt[s], c);
-                atomicAdd(&t.sumf[s], f);
-                return true;
-            }
-            atomicSub(t.occ, 1u);
         }
         s = (s + 1) & (C - 1);
     }
@@ -383,8 +380,8 @@ __device__ __forceinline__ int ct_lookup(const CountTable &t, uint32_t key) {
     const uint32_t C = 1u << t.bits;
     if (key == kEmptyKey) return t.cnt[C] ? (int)C : -1;
     uint32_t s = slot_hash(key, t.bits);
-    for (uint32_t probe = 0; probe < C; probe++) {
-        uint32_t k = t.keys[s];
+    for (uint32_t probe = 0; probe < kMaxProbe; probe++) {
+        const uint32_t k = t.keys[s];
         if (k == key) return (int)s;
         if (k == kEmptyKey) return -1;
         s = (s + 1) & (C - 1);
@@ -393,25 +390,38 @@ __device__ __forceinline__ int ct_lookup(const CountTable &t, uint32_t key) {
 }
 
 // Warp-aggregated insert: lanes holding the same key combine (count, fr-sum)
-// and only the group leader touches the table.  All 32 lanes must call it.
+// and only the group leader touches the table; every member follows its
+// leader's outcome.  All 32 lanes must call it.
 __device__ __forceinline__ bool agg_insert(const CountTable &t, bool valid, uint32_t key, unsigned long long f) {
-    uint32_t gsize;
-    unsigned long long gsum;
-    const bool lead = warp_group(valid, key, f, true, &gsize, &gsum);
+    const unsigned full = 0xFFFFFFFFu;
+    const uint32_t lane = lane_id();
+    const unsigned active = __ballot_sync(full, valid);
+    unsigned grp = __match_any_sync(full, key) & active;
+    if (!valid) grp = 1u << lane;
+    const int leader = __ffs(grp) - 1;
+    const uint32_t gsize = __popc(grp);
+    unsigned long long gsum = f;
+    unsigned multi = __ballot_sync(full, valid && gsize > 1 && (int)lane == leader);
+    while (multi) {
+        const int ld = __ffs(multi) - 1;
+        multi &= multi - 1;
+        const unsigned m = __shfl_sync(full, grp, ld);
+        const unsigned long long sm = warp_sum_u64(((m >> lane) & 1u) ? f : 0ull);
+        if ((int)lane == ld) gsum = sm;
+    }
     bool ok = true;
-    if (lead) ok = ct_insert(t, key, gsize, gsum);
-    // every member follows its leader's outcome
-    const unsigned grp = __match_any_sync(0xFFFFFFFFu, key) & __ballot_sync(0xFFFFFFFFu, valid);
-    const int leader = valid ? __ffs(grp) - 1 : (int)lane_id();
-    return __shfl_sync(0xFFFFFFFFu, ok, leader);
+    if (valid && (int)lane == leader) ok = ct_insert(t, key, gsize, gsum);
+    return __shfl_sync(full, ok, leader);
 }
+
+constexpr int kJoinPer = 8;   // elements per thread per tile (independent loads in flight)
 
 __global__ void __launch_bounds__(kJoinThreads)
 bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
                          const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t table_bits) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ uint32_t occ, novf;
+    __shared__ uint32_t novf;
     const uint32_t b = blockIdx.x;
     const uint32_t nR = cnt[b], nS = cnt[B + b];
     if (nR == 0 || nS == 0) return;
@@ -423,8 +433,7 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
     t.keys = reinterpret_cast<uint32_t *>(t.sumf + C + 1);
     t.cnt = t.keys + C + 1;
     t.bits = table_bits;
-    t.limit = C - C / 4;
-    t.occ = &occ;
+    const uint32_t tile = kJoinPer * blockDim.x;
 
     unsigned long long count = 0, prod = 0;
     uint32_t n = nR;
@@ -434,24 +443,44 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
             t.cnt[i] = 0;
             t.sumf[i] = 0;
         }
-        if (threadIdx.x == 0) { occ = 0; novf = 0; }
+        if (threadIdx.x == 0) novf = 0;
         __syncthreads();
-        for (uint32_t base = 0; base < n; base += blockDim.x) {
-            const uint32_t i = base + threadIdx.x;
-            const bool valid = i < n;
-            const uint64_t e = valid ? Rb[i] : 0;
+        // build: kJoinPer independent loads per thread, then insert them
+        for (uint32_t base = 0; base < n; base += tile) {
+            uint64_t e[kJoinPer];
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t i = base + k * blockDim.x + threadIdx.x;
+                e[k] = i < n ? Rb[i] : 0ull;
+            }
             __syncthreads();   // every read of this tile precedes any overflow write
-            const uint32_t key = (uint32_t)e;
-            const bool ok = agg_insert(t, valid, key, valid ? sjbg_fr((uint32_t)(e >> 32)) : 0ull);
-            if (valid && !ok) Rb[atomicAdd(&novf, 1u)] = e;
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t i = base + k * blockDim.x + threadIdx.x;
+                const bool valid = i < n;
+                const bool ok = agg_insert(t, valid, (uint32_t)e[k], valid ? sjbg_fr((uint32_t)(e[k] >> 32)) : 0ull);
+                if (valid && !ok) Rb[atomicAdd(&novf, 1u)] = e[k];
+            }
         }
         __syncthreads();
-        for (uint32_t j = threadIdx.x; j < nS; j += blockDim.x) {
-            const uint64_t e = Sb[j];
-            const int s = ct_lookup(t, (uint32_t)e);
-            if (s >= 0) {
-                count += t.cnt[s];
-                prod += t.sumf[s] * sjbg_gs((uint32_t)(e >> 32));
+        // probe: the same independent-load tiling, no barriers needed
+        for (uint32_t base = 0; base < nS; base += tile) {
+            uint64_t e[kJoinPer];
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t j = base + k * blockDim.x + threadIdx.x;
+                e[k] = j < nS ? Sb[j] : ~0ull;
+            }
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t j = base + k * blockDim.x + threadIdx.x;
+                if (j < nS) {
+                    const int s = ct_lookup(t, (uint32_t)e[k]);
+                    if (s >= 0) {
+                        count += t.cnt[s];
+                        prod += t.sumf[s] * sjbg_gs((uint32_t)(e[k] >> 32));
+                    }
+                }
             }
         }
         __syncthreads();

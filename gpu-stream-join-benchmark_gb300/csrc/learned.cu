@@ -172,7 +172,21 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             __syncthreads();
         }
     }
-    if (threadIdx.x == 0) n_heavy_s = min(nc, max_heavy);
+    if (threadIdx.x == 0) {
+        // largest first, a candidate is heavy while its sampled count exceeds an
+        // eighth of one bucket's share of the mass that is still light
+        const uint64_t P = 1ull << s.log2_buckets;
+        uint64_t light = s.m;
+        uint32_t h = 0;
+        const uint32_t lim = min(nc, max_heavy);
+        while (h < lim) {
+            const uint64_t c = sc[h] >> 32;
+            if (c * 8 * P <= light) break;
+            light -= c;
+            h++;
+        }
+        n_heavy_s = h;
+    }
     __syncthreads();
     const uint32_t nh = n_heavy_s;
     for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) {
@@ -221,10 +235,18 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         const double x = (double)(j + 1) / kBins, y = (double)hw[j] * invt;
         sx += x; sy += y; sxx += x * x; sxy += x * y;
     }
-    atomicAdd(&rootsum[0], sx);
-    atomicAdd(&rootsum[1], sy);
-    atomicAdd(&rootsum[2], sxx);
-    atomicAdd(&rootsum[3], sxy);
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
+        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+        sxx += __shfl_xor_sync(0xFFFFFFFFu, sxx, o);
+        sxy += __shfl_xor_sync(0xFFFFFFFFu, sxy, o);
+    }
+    if (lane_id() == 0) {
+        atomicAdd(&rootsum[0], sx);
+        atomicAdd(&rootsum[1], sy);
+        atomicAdd(&rootsum[2], sxx);
+        atomicAdd(&rootsum[3], sxy);
+    }
     __syncthreads();
     const double nn = kBins;
     const double den = nn * rootsum[2] - rootsum[0] * rootsum[0];
@@ -238,25 +260,71 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     };
 
     // ---- leaf lines, pass 1: counts and means; pass 2: centred products
-    for (uint32_t i = 0; i < per; i++) {
-        const uint32_t j = b0 + i;
-        const float x = (float)(j + 1) / kBins, y = (float)hw[j] * invt;
-        const int l = leaf_of(x);
-        atomicAdd(&ls[l][0], 1.0f);
-        atomicAdd(&ls[l][1], x);
-        atomicAdd(&ls[l][2], y);
-        atomicMin(reinterpret_cast<int *>(&lmin[l]), __float_as_int(y));   // y >= 0: int order == float order
-        atomicMax(reinterpret_cast<int *>(&lmax[l]), __float_as_int(y));
+    // a thread's bins are consecutive, so they fall into one or two leaves:
+    // sums are kept in registers per run of equal leaves and flushed on change
+    {
+        int cur = -1;
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f, mn = 2.f, mxv = -1.f;
+        for (uint32_t i = 0; i <= per; i++) {
+            int l = -1;
+            float x = 0.f, y = 0.f;
+            if (i < per) {
+                const uint32_t j = b0 + i;
+                x = (float)(j + 1) / kBins;
+                y = (float)hw[j] * invt;
+                l = leaf_of(x);
+            }
+            if (l != cur) {
+                if (cur >= 0) {
+                    atomicAdd(&ls[cur][0], c0);
+                    atomicAdd(&ls[cur][1], c1);
+                    atomicAdd(&ls[cur][2], c2);
+                    atomicMin(reinterpret_cast<int *>(&lmin[cur]), __float_as_int(mn));  // y >= 0: int order == float order
+                    atomicMax(reinterpret_cast<int *>(&lmax[cur]), __float_as_int(mxv));
+                }
+                cur = l;
+                c0 = c1 = c2 = 0.f;
+                mn = 2.f;
+                mxv = -1.f;
+            }
+            if (l >= 0) {
+                c0 += 1.f; c1 += x; c2 += y;
+                mn = fminf(mn, y);
+                mxv = fmaxf(mxv, y);
+            }
+        }
     }
     __syncthreads();
-    for (uint32_t i = 0; i < per; i++) {
-        const uint32_t j = b0 + i;
-        const float x = (float)(j + 1) / kBins, y = (float)hw[j] * invt;
-        const int l = leaf_of(x);
-        const float n = ls[l][0];
-        const float dx = x - ls[l][1] / n, dy = y - ls[l][2] / n;
-        atomicAdd(&ls[l][3], dx * dy);
-        atomicAdd(&ls[l][4], dx * dx);
+    {
+        int cur = -1;
+        float sxy = 0.f, sxx = 0.f, mx = 0.f, my = 0.f;
+        for (uint32_t i = 0; i <= per; i++) {
+            int l = -1;
+            float x = 0.f, y = 0.f;
+            if (i < per) {
+                const uint32_t j = b0 + i;
+                x = (float)(j + 1) / kBins;
+                y = (float)hw[j] * invt;
+                l = leaf_of(x);
+            }
+            if (l != cur) {
+                if (cur >= 0) {
+                    atomicAdd(&ls[cur][3], sxy);
+                    atomicAdd(&ls[cur][4], sxx);
+                }
+                cur = l;
+                sxy = sxx = 0.f;
+                if (l >= 0) {
+                    mx = ls[l][1] / ls[l][0];
+                    my = ls[l][2] / ls[l][0];
+                }
+            }
+            if (l >= 0) {
+                const float dx = x - mx, dy = y - my;
+                sxy += dx * dy;
+                sxx += dx * dx;
+            }
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -340,7 +408,7 @@ uint32_t learned_log2_buckets(sjbg_handle *h, uint64_t n_left) {
 int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinPlan *plan, uint32_t n,
                     WinPlan *dPlan, const LearnedModel **dModels, bool allow_heavy) {
     const float rate = h->cfg.sample_rate > 0.0f ? h->cfg.sample_rate : 0.01f;
-    const float bound = h->cfg.overflow_bound > 0.0f ? h->cfg.overflow_bound : 4.0f;
+    const float bound = h->cfg.overflow_bound > 0.0f ? h->cfg.overflow_bound : 8.0f;
     const uint32_t leaves = h->cfg.learned_leaves ? std::min(h->cfg.learned_leaves, kMaxLeaves) : kMaxLeaves;
     std::vector<SampleWin> sw(n);
     uint64_t table_total = 0;
@@ -363,8 +431,9 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         table_total += (uint64_t)1 << lg;
         s.log2_buckets = p.log2_buckets;
         const uint64_t P = (uint64_t)1 << p.log2_buckets;
-        // heavy: sampled mass above half of one bucket's fair share (and >= 4 hits)
-        s.thresh = (uint32_t)std::max<uint64_t>(4, m / (2 * P));
+        // heavy candidates: keys sampled at least max(4, m / 64P) times; the fit
+        // keeps those that exceed an eighth of a bucket of the remaining light mass
+        s.thresh = (uint32_t)std::max<uint64_t>(4, m / (64 * P));
         max_m = std::max(max_m, s.m);
     }
     const size_t swB = sizeof(SampleWin) * n, scB = sizeof(SampleScratch) * n;

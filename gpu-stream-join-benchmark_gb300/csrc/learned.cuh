@@ -18,8 +18,8 @@
 namespace sjbg {
 
 constexpr uint32_t kMaxLeaves = 256;
-constexpr uint32_t kMaxHeavy = 256;
-constexpr uint32_t kHeavySlots = 512;          // shared-memory heavy-key table
+constexpr uint32_t kMaxHeavy = 512;
+constexpr uint32_t kHeavySlots = 1024;         // shared-memory heavy-key table
 constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu; // classify(): heavy key marker
 
 struct LearnedModel {
@@ -54,7 +54,7 @@ struct HeavySet {
     uint32_t idx[kHeavySlots];
 };
 
-__device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, 9); }
+__device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, 10); }
 
 // Cooperative load of a model's heavy keys (all threads; ends with a barrier).
 __device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel *m) {

@@ -137,7 +137,7 @@ typedef struct sjbg_config {
     uint32_t radix_bits;            /* partition fan-out log2 (<= 14); 0 = about 4096 left tuples per bucket */
     uint32_t learned_leaves;        /* leaf segments of the CDF model, 0 = 256 */
     float sample_rate;              /* learned: fraction of tuples sampled, 0 = 0.01 */
-    float overflow_bound;           /* learned: worst partition / mean partition allowed, 0 = 4 */
+    float overflow_bound;           /* learned: worst partition / mean partition allowed, 0 = 8 */
     int32_t device;                 /* CUDA device ordinal */
     uint64_t hbm_budget_bytes;      /* streaming admission budget, 0 = no limit */
 } sjbg_config;
