@@ -299,7 +299,8 @@ def main():
         "config": {"workload": args.workload, "windows": nwin, "tuples_per_window_per_stream": W,
                    "key_domain": D, "zipf_z": z, "partitioner": "learned (256 leaves, 1% sample)",
                    "learned_fanout": "auto (about 4096 left tuples per bucket)",
-                   "l2": "inputs larger than L2 (4 GiB per step)" if total * 32 > (256 << 20) else "L2-resident"},
+                   "l2": (f"inputs larger than L2 ({total * 32 >> 20} MiB per step)" if total * 32 > (129 << 20)
+                          else "L2-resident inputs")},
         "plain": {"value": tuples / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                   "partitioner": f"radix 2^{plain_bits}" if plain_bits else "radix, auto fan-out"},
         "radix_same_fanout_as_learned": {"value": tuples / (ms_radix_auto * 1e-3), "ms_per_step": ms_radix_auto},

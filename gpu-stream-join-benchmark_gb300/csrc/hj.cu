@@ -123,30 +123,57 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         heavy_set_load(hs, cls.m);   // ends with a barrier
     }
     __syncthreads();
-    for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
-        const uint32_t i = i0 + threadIdx.x;
+    constexpr int kPer = kTile / kPartThreads;
+    uint4 v[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {   // all of the thread's loads in flight before any use
+        const uint32_t i = threadIdx.x + k * kPartThreads;
+        v[k] = i < n ? __ldg(src + i) : make_uint4(0u, 0u, 0u, 0u);   // whole 16-byte tuple
+    }
+    // the hottest heavy keys (the fit orders heavy keys by sampled count) are
+    // accumulated in registers; other heavy keys with shared atomics
+    constexpr int kRegHeavy = 4;
+    uint32_t rc[kRegHeavy] = {0, 0, 0, 0};
+    unsigned long long rs[kRegHeavy] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const uint32_t i = threadIdx.x + k * kPartThreads;
         const bool valid = i < n;
-        uint32_t key = 0, val = 0;
-        if (valid) {
-            const uint4 v = __ldg(src + i);   // whole 16-byte tuple, one vector load
-            key = v.x;
-            val = v.y;
-        }
-        uint32_t hid = kHeavyBucket;
-        if (heavy && valid) hid = heavy_find(hs, key);
-        uint32_t gs;
-        unsigned long long gsum;
+        const uint32_t key = v[k].x, val = v[k].y;
         if (heavy) {
-            const bool hv = valid && hid != kHeavyBucket;
-            const unsigned long long f = hv ? (right ? sjbg_gs(val) : sjbg_fr(val)) : 0ull;
-            if (warp_group(hv, hid, f, true, &gs, &gsum)) {
-                atomicAdd(&hcnt[hid], gs);
-                atomicAdd(&hsum[hid], gsum);
+            const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
+            if (hid != kHeavyBucket) {
+                const unsigned long long f = right ? sjbg_gs(val) : sjbg_fr(val);
+                if (hid < kRegHeavy) {
+#pragma unroll
+                    for (int q = 0; q < kRegHeavy; q++)
+                        if (hid == (uint32_t)q) { rc[q]++; rs[q] += f; }
+                } else {
+                    atomicAdd(&hcnt[hid], 1u);
+                    atomicAdd(&hsum[hid], f);
+                }
+            } else if (valid) {
+                atomicAdd(&hist[cls.bucket(key)], 1u);   // light keys: balanced buckets
+            }
+        } else {
+            // plain partitioning: skewed keys hammer one bucket, so equal buckets
+            // of a warp are combined before the shared atomic
+            uint32_t gs;
+            unsigned long long gsum;
+            const uint32_t b = valid ? cls.bucket(key) : 0u;
+            if (warp_group(valid, b, 0ull, false, &gs, &gsum)) atomicAdd(&hist[b], gs);
+        }
+    }
+    if (heavy) {
+#pragma unroll
+        for (int q = 0; q < kRegHeavy; q++) {
+            const unsigned long long c = warp_sum_u64(rc[q]);
+            const unsigned long long sm = warp_sum_u64(rs[q]);
+            if (lane_id() == 0 && c) {
+                atomicAdd(&hcnt[q], (uint32_t)c);
+                atomicAdd(&hsum[q], sm);
             }
         }
-        const bool light = valid && hid == kHeavyBucket;
-        const uint32_t b = light ? cls.bucket(key) : 0u;
-        if (warp_group(light, b, 0ull, false, &gs, &gsum)) atomicAdd(&hist[b], gs);
     }
     __syncthreads();
     uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
@@ -299,14 +326,21 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
     uint64_t e[kPer];
     uint32_t bk[kPer], rk[kPer];
 #pragma unroll
+    for (int k = 0; k < kPer; k++) {   // all of the thread's loads in flight before any use
+        const uint32_t i = threadIdx.x + k * kPartThreads;
+        if (i < n) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(src + i));   // key and val only
+            e[k] = ((uint64_t)v.y << 32) | v.x;
+        }
+    }
+#pragma unroll
     for (int k = 0; k < kPer; k++) {
         const uint32_t i = threadIdx.x + k * kPartThreads;
         bk[k] = kHeavyBucket;
         if (i < n) {
-            const uint4 v = __ldg(src + i);
-            e[k] = ((uint64_t)v.y << 32) | v.x;
-            if (!heavy || heavy_find(hs, v.x) == kHeavyBucket) {
-                bk[k] = cls.bucket(v.x);
+            const uint32_t key = (uint32_t)e[k];
+            if (!heavy || heavy_find(hs, key) == kHeavyBucket) {
+                bk[k] = cls.bucket(key);
                 rk[k] = atomicAdd(&lcnt[bk[k]], 1u);
             }
         }

@@ -196,6 +196,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         atomicSub(&hw[bin_of(key_x(key, kmin, inv))], c);   // light histogram only
     }
     __syncthreads();
+    heavy_set_build(M.heavy_set, M.heavy_keys, nh);
 
     // ---- light CDF at bin upper edges: in-place exclusive scan, then cdf_j = incl_j / total
     const uint32_t per = kBins / blockDim.x;   // 64

@@ -22,11 +22,20 @@ constexpr uint32_t kMaxHeavy = 512;
 constexpr uint32_t kHeavySlots = 1024;         // shared-memory heavy-key table
 constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu; // classify(): heavy key marker
 
+// Shared-memory heavy-key set: slot -> (key, index); empty slots hold kEmptyKey
+// in the key and 0xFFFFFFFF in the index (the index distinguishes a heavy key
+// equal to 0xFFFFFFFF from an empty slot).
+struct HeavySet {
+    uint32_t keys[kHeavySlots];
+    uint32_t idx[kHeavySlots];
+};
+
 struct LearnedModel {
     float kmin, inv_range, root_a, root_b;
     uint32_t leaves, log2_buckets, fallback, n_heavy;
     float slope[kMaxLeaves], mean_x[kMaxLeaves], mean_y[kMaxLeaves], lo[kMaxLeaves], hi[kMaxLeaves];
     uint32_t heavy_keys[kMaxHeavy];
+    HeavySet heavy_set;   // built once by the fit, copied into shared memory by each CTA
 };
 
 // Per-window, per-heavy-key aggregates.
@@ -46,37 +55,35 @@ __device__ __forceinline__ uint32_t learned_bucket(const LearnedModel &m, uint32
     return b < P ? b : P - 1;
 }
 
-// Shared-memory heavy-key set: slot -> (key, index); empty slots hold kEmptyKey
-// in the key and 0xFFFFFFFF in the index (the index distinguishes a heavy key
-// equal to 0xFFFFFFFF from an empty slot).
-struct HeavySet {
-    uint32_t keys[kHeavySlots];
-    uint32_t idx[kHeavySlots];
-};
-
 __device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, 10); }
 
-// Cooperative load of a model's heavy keys (all threads; ends with a barrier).
-__device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel *m) {
+// Build a heavy-key set from keys[0..n) (one CTA; ends with a barrier).
+__device__ __forceinline__ void heavy_set_build(HeavySet &hs, const uint32_t *keys, uint32_t n) {
     for (uint32_t i = threadIdx.x; i < kHeavySlots; i += blockDim.x) {
         hs.keys[i] = kEmptyKey;
         hs.idx[i] = 0xFFFFFFFFu;
     }
     __syncthreads();
-    if (m && !m->fallback) {
-        for (uint32_t h = threadIdx.x; h < m->n_heavy; h += blockDim.x) {
-            uint32_t key = m->heavy_keys[h];
-            uint32_t s = heavy_slot(key);
-            for (uint32_t p = 0; p < kHeavySlots; p++) {
-                // claim by index, which is unique per heavy key
-                if (atomicCAS(&hs.idx[s], 0xFFFFFFFFu, h) == 0xFFFFFFFFu) {
-                    hs.keys[s] = key;
-                    break;
-                }
-                s = (s + 1) & (kHeavySlots - 1);
+    for (uint32_t h = threadIdx.x; h < n; h += blockDim.x) {
+        const uint32_t key = keys[h];
+        uint32_t s = heavy_slot(key);
+        for (uint32_t p = 0; p < kHeavySlots; p++) {
+            // claim by index, which is unique per heavy key
+            if (atomicCAS(&hs.idx[s], 0xFFFFFFFFu, h) == 0xFFFFFFFFu) {
+                hs.keys[s] = key;
+                break;
             }
+            s = (s + 1) & (kHeavySlots - 1);
         }
     }
+    __syncthreads();
+}
+
+// Copy a model's prebuilt heavy-key set into shared memory (all threads; ends with a barrier).
+__device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel *m) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(&m->heavy_set);
+    uint4 *dst = reinterpret_cast<uint4 *>(&hs);
+    for (uint32_t i = threadIdx.x; i < sizeof(HeavySet) / 16; i += blockDim.x) dst[i] = src[i];
     __syncthreads();
 }
 

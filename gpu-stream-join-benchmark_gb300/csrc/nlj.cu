@@ -1,0 +1,177 @@
+// nlj.cu - lazy nested-loop join (sm_103a).
+//
+// Replaces the reference's lazy GPU nested-loop family
+// (src/sjb/windowing/lazy/executor/GPU/GPU_NLJ.cu:28-145 and its NoOutput /
+// CountKernel / EstimatedSelectivity / Bitmap variants; one thread per pair
+// with atomicAggInc, CudaUtils.cuh:8-14), whose matching rule is the lazy
+// CPU_NLJ's (src/sjb/windowing/lazy/executor/CPU/CPU_NLJ.cpp:11-32): every
+// (left, right) pair of the window is compared.
+//
+// Design: each thread keeps kLReg left keys in registers; the CTA streams the
+// window's right side through shared memory in chunks of kChunk keys (SoA:
+// keys and vals, extracted from the 16-byte tuples with vector loads).  The
+// hot loop reads four right keys with one 128-bit shared load (a broadcast)
+// and folds key equality into one predicate per thread (p |= a == b); every
+// 64 right keys the warp votes (__any_sync) and only a warp that saw a match
+// re-walks those 64 keys exactly: count, prod and xor checksums, and the
+// (left.val, right.val) pairs appended with one atomic per warp
+// (__ballot_sync/__popc-style warp aggregation of the reference's atomicAggInc).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "runtime.h"
+
+namespace sjbg {
+
+constexpr int kNljThreads = 256;
+constexpr int kLReg = 8;                         // left keys per thread
+constexpr uint32_t kLTile = kNljThreads * kLReg;  // left tuples per CTA
+constexpr uint32_t kChunk = 2048;                // right tuples per shared-memory chunk
+constexpr uint32_t kRSplit = 16384;              // right tuples per CTA
+constexpr uint32_t kVote = 64;                   // right keys between warp votes
+
+struct NljItem {
+    uint32_t win, l0, r0, pad;
+};
+
+template <bool kEnum, bool kPairs>
+__global__ void __launch_bounds__(kNljThreads)
+nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
+           const NljItem *__restrict__ items, WinAcc *__restrict__ acc, sjbg_pair *__restrict__ pairs) {
+    __shared__ __align__(16) uint32_t rkeys[kChunk];
+    __shared__ __align__(16) uint32_t rvals[kChunk];
+    const NljItem it = items[blockIdx.x];
+    const WinPlan wp = wins[it.win];
+    const sjbg_tuple *Lw = L + wp.left_off;
+    const sjbg_tuple *Rw = R + wp.right_off;
+    const uint32_t nL = (uint32_t)wp.n_left, nR = (uint32_t)wp.n_right;
+
+    uint32_t lk[kLReg], lv[kLReg];
+    uint32_t lvalid = 0;
+    uint32_t fill = 0;
+#pragma unroll
+    for (int a = 0; a < kLReg; a++) {
+        const uint32_t li = it.l0 + a * kNljThreads + threadIdx.x;
+        if (li < nL) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(Lw + li));
+            lk[a] = t.x;
+            lv[a] = t.y;
+            lvalid |= 1u << a;
+            fill = t.x;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < kLReg; a++)
+        if (!((lvalid >> a) & 1u)) { lk[a] = fill; lv[a] = 0; }   // invalid slots only cause false alarms
+
+    unsigned long long count = 0, xr = 0, prod = 0;
+    const uint32_t r_end = min(nR, it.r0 + kRSplit);
+    const uint64_t pcap = kPairs ? wp.pairs_cap : 0;
+    sjbg_pair *pout = kPairs ? pairs + wp.pairs_off : nullptr;
+
+    for (uint32_t c0 = it.r0; c0 < r_end; c0 += kChunk) {
+        const uint32_t m = min(kChunk, r_end - c0);
+        const uint32_t mpad = (m + kVote - 1) / kVote * kVote;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < mpad; i += kNljThreads) {
+            if (i < m) {
+                const uint2 t = __ldg(reinterpret_cast<const uint2 *>(Rw + c0 + i));
+                rkeys[i] = t.x;
+                rvals[i] = t.y;
+            } else {
+                rkeys[i] = lk[0];   // padding: bounds are re-checked in the exact path
+                rvals[i] = 0;
+            }
+        }
+        __syncthreads();
+        const uint4 *rk4 = reinterpret_cast<const uint4 *>(rkeys);
+        for (uint32_t r = 0; r < mpad; r += kVote) {
+            bool p = false;
+#pragma unroll 4
+            for (uint32_t q = 0; q < kVote / 4; q++) {
+                const uint4 k4 = rk4[(r >> 2) + q];
+#pragma unroll
+                for (int a = 0; a < kLReg; a++)
+                    p |= (lk[a] == k4.x) | (lk[a] == k4.y) | (lk[a] == k4.z) | (lk[a] == k4.w);
+            }
+            if (!__any_sync(0xFFFFFFFFu, p)) continue;
+            // exact path for this group of kVote right keys (warp-uniform)
+            const uint32_t qe = min(r + kVote, m);
+            uint32_t mine = 0;
+            for (uint32_t q = r; q < qe; q++) {
+                const uint32_t k = rkeys[q];
+#pragma unroll
+                for (int a = 0; a < kLReg; a++) {
+                    if (((lvalid >> a) & 1u) && lk[a] == k) {
+                        const uint32_t sv = rvals[q];
+                        mine++;
+                        prod += sjbg_fr(lv[a]) * sjbg_gs(sv);
+                        if (kEnum) xr ^= sjbg_pair_hash(lv[a], sv);
+                    }
+                }
+            }
+            count += mine;
+            if (kPairs) {
+                uint32_t tot;
+                const uint32_t ex = warp_excl_scan(mine, &tot);
+                unsigned long long base = 0;
+                if (lane_id() == 0 && tot) base = atomicAdd(&acc[it.win].npairs, (unsigned long long)tot);
+                base = __shfl_sync(0xFFFFFFFFu, base, 0) + ex;
+                for (uint32_t q = r; q < qe && mine; q++) {
+                    const uint32_t k = rkeys[q];
+#pragma unroll
+                    for (int a = 0; a < kLReg; a++) {
+                        if (((lvalid >> a) & 1u) && lk[a] == k) {
+                            if (base < pcap) pout[base] = sjbg_pair{lv[a], rvals[q]};
+                            base++;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    flush_acc(&acc[it.win], count, xr, prod);
+}
+
+int nlj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                   sjbg_pair *dPairs, WinAcc *acc, bool enumerate) {
+    if (n == 0) return SJBG_OK;
+    std::vector<WinPlan> plan(n);
+    std::vector<NljItem> items;
+    for (uint32_t w = 0; w < n; w++) {
+        const WinHost &wh = wins[w];
+        if (wh.n_left >= 0xFFFFFFFFull || wh.n_right >= 0xFFFFFFFFull)
+            return fail(h, SJBG_E_CAPACITY, "nested-loop windows are limited to 2^32 tuples per side");
+        WinPlan &p = plan[w];
+        std::memset(&p, 0, sizeof(p));
+        p.left_off = wh.left_off; p.n_left = wh.n_left; p.right_off = wh.right_off; p.n_right = wh.n_right;
+        p.pairs_off = wh.pairs_off; p.pairs_cap = dPairs ? wh.pairs_cap : 0;
+        p.model = 0xFFFFFFFFu;
+        for (uint64_t l0 = 0; l0 < wh.n_left; l0 += kLTile)
+            for (uint64_t r0 = 0; r0 < wh.n_right; r0 += kRSplit) items.push_back({w, (uint32_t)l0, (uint32_t)r0, 0});
+    }
+    if (items.empty()) return SJBG_OK;
+    const size_t planB = sizeof(WinPlan) * n, itB = sizeof(NljItem) * items.size();
+    uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 0, planB + itB));
+    uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_WIN_PLAN, planB + itB));
+    if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "nested-loop plan");
+    std::memcpy(hst, plan.data(), planB);
+    std::memcpy(hst + planB, items.data(), itB);
+    SJBG_CK(h, cudaMemcpyAsync(dev, hst, planB + itB, cudaMemcpyHostToDevice, h->stream));
+    const WinPlan *dPlan = reinterpret_cast<const WinPlan *>(dev);
+    const NljItem *dItems = reinterpret_cast<const NljItem *>(dev + planB);
+    const dim3 grid((uint32_t)items.size());
+    if (dPairs)
+        SJBG_CK(h, launch(h, "nlj_pairs", nlj_kernel<true, true>, grid, dim3(kNljThreads), 0, dL, dR, dPlan, dItems,
+                          acc, dPairs));
+    else if (enumerate)
+        SJBG_CK(h, launch(h, "nlj_xor", nlj_kernel<true, false>, grid, dim3(kNljThreads), 0, dL, dR, dPlan, dItems,
+                          acc, dPairs));
+    else
+        SJBG_CK(h, launch(h, "nlj_count", nlj_kernel<false, false>, grid, dim3(kNljThreads), 0, dL, dR, dPlan, dItems,
+                          acc, dPairs));
+    return SJBG_OK;
+}
+
+}  // namespace sjbg

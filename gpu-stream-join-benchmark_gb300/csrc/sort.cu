@@ -1,0 +1,424 @@
+// sort.cu - segmented LSD radix sort (8-bit digits) of (key, val) pairs and
+// segmented prefix sums, for the sort-merge join (sm_103a).
+//
+// One pass = three launches over all segments of a batch:
+//   rs_upsweep    per 4096-key tile: digit histogram (shared atomics)
+//   rs_scan       per segment: exclusive scan of its [256 digits x tiles]
+//                 count block, digit-major, so tile t's digit d lands after all
+//                 smaller digits and after digit d of tiles < t (stability)
+//   rs_downsweep  per tile: the tile's keys and vals are staged in shared
+//                 memory by TMA bulk copies (cp.async.bulk, mbarrier with a
+//                 bounded wait); stable ranks come from warp-private digit
+//                 counters and __match_any_sync; the tile is reordered in
+//                 shared memory and written as contiguous per-digit runs.
+// The reference's GPU sort-merge join uses a counting sort by key with
+// unstable atomics instead (src/sjb/windowing/lazy/executor/GPU/GPU_SMJ.cu:19-32).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "sort.cuh"
+
+namespace sjbg {
+
+constexpr int kSortThreads = 512;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr uint32_t kDigits = 256;
+
+SortPlan sort_plan(const uint64_t *n, const uint64_t *src, uint32_t k) {
+    SortPlan p;
+    p.segs.resize(k);
+    uint64_t off = 0;
+    uint32_t tiles = 0;
+    for (uint32_t s = 0; s < k; s++) {
+        const uint64_t padded = (n[s] + 1 + kSortTile - 1) / kSortTile * kSortTile;
+        p.segs[s] = SortSeg{off, src[s], (uint32_t)n[s], tiles, (uint32_t)(padded / kSortTile), 0};
+        off += padded;
+        tiles += (uint32_t)(padded / kSortTile);
+    }
+    p.tiles = tiles;
+    p.elems = off;
+    return p;
+}
+
+// ------------------------------------------------------------------ TMA bulk staging
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// 1-D bulk copy global -> shared (16-byte aligned addresses, size multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Bounded wait on phase `parity`; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < (1u << 26); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// ------------------------------------------------------------------ kernels
+// Segments [0, split) read srcA, the others srcB.
+__global__ void __launch_bounds__(256)
+sort_extract_kernel(const sjbg_tuple *__restrict__ srcA, const sjbg_tuple *__restrict__ srcB, uint32_t split,
+                    const SortSeg *__restrict__ segs, uint32_t nseg, uint32_t *__restrict__ keys,
+                    uint32_t *__restrict__ vals) {
+    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const SortSeg sg = segs[s];
+    const sjbg_tuple *src = s < split ? srcA : srcB;
+    const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
+    for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x) {
+        const uint32_t li = base + i;
+        uint32_t k = 0xFFFFFFFFu, v = 0;
+        if (li < sg.n) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(src + sg.src + li));
+            k = t.x;
+            v = t.y;
+        }
+        keys[sg.off + li] = k;
+        vals[sg.off + li] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, uint32_t nseg,
+                uint32_t *__restrict__ out) {
+    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const SortSeg sg = segs[s];
+    const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
+    uint32_t m = 0;
+    for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x)
+        if (base + i < sg.n) m = max(m, keys[sg.off + base + i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if (lane_id() == 0 && m) atomicMax(out, m);
+}
+
+// counts block of segment s: counts[tile0 * 256 + d * ntiles + t_local]
+__global__ void __launch_bounds__(256)
+rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, uint32_t nseg, uint32_t shift,
+                  uint32_t *__restrict__ counts) {
+    __shared__ uint32_t hist[kDigits];
+    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const SortSeg sg = segs[s];
+    const uint32_t tl = blockIdx.x - sg.tile0;
+    const uint32_t base = tl * kSortTile;
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    const uint4 *k4 = reinterpret_cast<const uint4 *>(keys + sg.off + base);
+    constexpr int kPer = kSortTile / 4 / 256;   // 4 vectors per thread
+    uint4 v[kPer];
+#pragma unroll
+    for (int q = 0; q < kPer; q++) v[q] = __ldg(k4 + threadIdx.x + q * 256);
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+        const uint32_t e0 = base + 4 * (threadIdx.x + q * 256);
+        const uint32_t kk[4] = {v[q].x, v[q].y, v[q].z, v[q].w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const bool valid = e0 + c < sg.n;
+            const uint32_t d = valid ? (kk[c] >> shift) & 0xFFu : 0u;
+            // skewed keys share digits: combine equal digits of the warp first
+            const unsigned grp = __match_any_sync(0xFFFFFFFFu, valid ? d : 0x100u);
+            if (valid && lane_id() == (uint32_t)(__ffs(grp) - 1)) atomicAdd(&hist[d], (uint32_t)__popc(grp));
+        }
+    }
+    __syncthreads();
+    counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl] = hist[threadIdx.x];
+}
+
+// One CTA per segment: exclusive scan of its 256 * ntiles counts in place.
+__global__ void __launch_bounds__(1024)
+rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t carry_s;
+    const SortSeg sg = segs[blockIdx.x];
+    uint32_t *c = counts + (uint64_t)sg.tile0 * kDigits;
+    const uint32_t n = kDigits * sg.ntiles;
+    if (threadIdx.x == 0) carry_s = 0;
+    __syncthreads();
+    constexpr uint32_t kItems = 4;
+    for (uint32_t base = 0; base < n; base += blockDim.x * kItems) {
+        uint32_t v[kItems], s = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kItems; k++) {
+            const uint32_t i = base + threadIdx.x * kItems + k;
+            v[k] = i < n ? c[i] : 0;
+            s += v[k];
+        }
+        uint32_t wt;
+        const uint32_t ex = warp_excl_scan(s, &wt);
+        if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
+        __syncthreads();
+        if (warp_id() == 0) {
+            const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0;
+            uint32_t tt;
+            warp_tot[lane_id()] = warp_excl_scan(x, &tt);
+        }
+        __syncthreads();
+        uint32_t run = carry_s + warp_tot[warp_id()] + ex;
+#pragma unroll
+        for (uint32_t k = 0; k < kItems; k++) {
+            const uint32_t i = base + threadIdx.x * kItems + k;
+            if (i < n) c[i] = run;
+            run += v[k];
+        }
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry_s = run;
+        __syncthreads();
+    }
+}
+
+struct DownSmem {
+    uint32_t in_keys[kSortTile];
+    uint32_t in_vals[kSortTile];
+    uint32_t out_keys[kSortTile];
+    uint32_t out_vals[kSortTile];
+    uint32_t wcnt[kSortWarps][kDigits + 1];   // per-warp digit counters (+1: invalid slots)
+    uint32_t loc[kDigits];                     // tile-local digit offsets
+    uint32_t gofs[kDigits];                    // global digit offsets of this tile
+    uint32_t warp_tot[32];
+    uint64_t bar;
+};
+
+__global__ void __launch_bounds__(kSortThreads)
+rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                    uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
+                    const SortSeg *__restrict__ segs, uint32_t nseg, uint32_t shift,
+                    const uint32_t *__restrict__ counts, uint32_t *__restrict__ status) {
+    extern __shared__ __align__(128) uint8_t smem_raw[];
+    DownSmem &sm = *reinterpret_cast<DownSmem *>(smem_raw);
+    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const SortSeg sg = segs[s];
+    const uint32_t tl = blockIdx.x - sg.tile0;
+    const uint32_t base = tl * kSortTile;
+    const uint32_t n = sg.n > base ? min(kSortTile, sg.n - base) : 0u;
+    const uint32_t w = warp_id(), lane = lane_id();
+
+    if (threadIdx.x == 0) mbar_init(&sm.bar, 1);
+    for (uint32_t i = threadIdx.x; i < kSortWarps * (kDigits + 1); i += kSortThreads) (&sm.wcnt[0][0])[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&sm.bar, 2 * kSortTile * 4);
+        bulk_g2s(sm.in_keys, keys + sg.off + base, kSortTile * 4, &sm.bar);
+        bulk_g2s(sm.in_vals, vals + sg.off + base, kSortTile * 4, &sm.bar);
+    }
+    if (threadIdx.x < kDigits)
+        sm.gofs[threadIdx.x] = counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl];
+    // every thread waits (bounded); the block leaves together if any gave up
+    const bool arrived = mbar_wait(&sm.bar, 0);
+    if (!__syncthreads_and(arrived)) {
+        if (threadIdx.x == 0) atomicOr(status, kErrTimeout);
+        return;
+    }
+
+    // stable warp-local ranks: warp w owns tile positions [w*256, w*256+256),
+    // item k of lane l is position w*256 + k*32 + l (k-major = tile order)
+    constexpr int kItems = kSortTile / kSortThreads;   // 8
+    uint32_t rank[kItems], dig[kItems];
+    const unsigned lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+        const uint32_t pos = w * (kSortTile / kSortWarps) + k * 32 + lane;
+        const uint32_t d = pos < n ? (sm.in_keys[pos] >> shift) & 0xFFu : kDigits;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t cur = sm.wcnt[w][d];
+        __syncwarp();
+        rank[k] = cur + __popc(peers & lt_mask);
+        dig[k] = d;
+        if (lane == (uint32_t)(__ffs(peers) - 1)) sm.wcnt[w][d] = cur + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: exclusive scan over warps, tile total in `loc`
+    if (threadIdx.x < kDigits) {
+        uint32_t run = 0;
+        for (int ww = 0; ww < kSortWarps; ww++) {
+            const uint32_t c = sm.wcnt[ww][threadIdx.x];
+            sm.wcnt[ww][threadIdx.x] = run;
+            run += c;
+        }
+        sm.loc[threadIdx.x] = run;
+    }
+    __syncthreads();
+    // exclusive scan of the 256 digit totals (8 warps x 32 digits)
+    if (threadIdx.x < kDigits) {
+        const uint32_t x = sm.loc[threadIdx.x];
+        uint32_t tot;
+        const uint32_t ex = warp_excl_scan(x, &tot);
+        if (lane == 31) sm.warp_tot[w] = ex + x;
+        __syncwarp();
+        sm.loc[threadIdx.x] = ex;   // partial; warp offsets added below
+    }
+    __syncthreads();
+    if (threadIdx.x < kDigits) {
+        uint32_t add = 0;
+        for (uint32_t ww = 0; ww < w; ww++) add += sm.warp_tot[ww];
+        sm.loc[threadIdx.x] += add;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+        const uint32_t pos = w * (kSortTile / kSortWarps) + k * 32 + lane;
+        if (pos < n) {
+            const uint32_t d = dig[k];
+            const uint32_t p = sm.loc[d] + sm.wcnt[w][d] + rank[k];
+            sm.out_keys[p] = sm.in_keys[pos];
+            sm.out_vals[p] = sm.in_vals[pos];
+        }
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < n; j += kSortThreads) {
+        const uint32_t k = sm.out_keys[j];
+        const uint32_t d = (k >> shift) & 0xFFu;
+        const uint64_t dst = sg.off + sm.gofs[d] + (j - sm.loc[d]);
+        keys_out[dst] = k;
+        vals_out[dst] = sm.out_vals[j];
+    }
+}
+
+// ---- segmented exclusive prefix of fr(val): tile sums, per-segment scan of the
+// ---- tile sums, per-tile scan plus offset
+__global__ void __launch_bounds__(256)
+fr_tile_sum_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, uint32_t nseg,
+                   unsigned long long *__restrict__ tsum) {
+    __shared__ unsigned long long ws[8];
+    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const SortSeg sg = segs[s];
+    const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
+    unsigned long long acc = 0;
+    for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x)
+        if (base + i < sg.n) acc += sjbg_fr(vals[sg.off + base + i]);
+    acc = warp_sum_u64(acc);
+    if (lane_id() == 0) ws[warp_id()] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int i = 0; i < 8; i++) t += ws[i];
+        tsum[blockIdx.x] = t;
+    }
+}
+
+__global__ void fr_seg_scan_kernel(unsigned long long *__restrict__ tsum, const SortSeg *__restrict__ segs) {
+    const SortSeg sg = segs[blockIdx.x];
+    if (threadIdx.x == 0) {
+        unsigned long long run = 0;
+        for (uint32_t t = 0; t < sg.ntiles; t++) {
+            const unsigned long long v = tsum[sg.tile0 + t];
+            tsum[sg.tile0 + t] = run;
+            run += v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, uint32_t nseg,
+                    const unsigned long long *__restrict__ tsum, unsigned long long *__restrict__ out) {
+    __shared__ unsigned long long wsum[8];
+    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const SortSeg sg = segs[s];
+    const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
+    constexpr uint32_t kPer = kSortTile / 256;   // 16 consecutive elements per thread
+    const uint32_t b0 = threadIdx.x * kPer;
+    unsigned long long loc = 0;
+    for (uint32_t i = 0; i < kPer; i++)
+        if (base + b0 + i < sg.n) loc += sjbg_fr(vals[sg.off + base + b0 + i]);
+    // exclusive scan of loc across the block
+    unsigned long long x = loc;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane_id() >= (uint32_t)o) x += y;
+    }
+    if (lane_id() == 31) wsum[warp_id()] = x;
+    __syncthreads();
+    unsigned long long wofs = 0;
+    for (uint32_t ww = 0; ww < warp_id(); ww++) wofs += wsum[ww];
+    unsigned long long run = tsum[blockIdx.x] + wofs + x - loc;
+    for (uint32_t i = 0; i < kPer; i++) {
+        const uint32_t li = base + b0 + i;
+        if (li <= sg.n) out[sg.off + li] = run;   // positions 0..n inclusive
+        if (li < sg.n) run += sjbg_fr(vals[sg.off + li]);
+    }
+}
+
+// ------------------------------------------------------------------ host drivers
+int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB, uint32_t split, const SortPlan &plan,
+                 const SortSeg *dSegs, uint32_t *keys, uint32_t *vals) {
+    SJBG_CK(h, launch(h, "sort_extract", sort_extract_kernel, dim3(plan.tiles), dim3(256), 0, srcA, srcB, split, dSegs,
+                      (uint32_t)plan.segs.size(), keys, vals));
+    return SJBG_OK;
+}
+
+int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
+                        uint32_t *keys2, uint32_t *vals2) {
+    const uint32_t nseg = (uint32_t)plan.segs.size();
+    uint32_t *dMax = static_cast<uint32_t *>(ws_get(h, WS_STATUS, 64));
+    uint32_t *counts = static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * plan.tiles));
+    uint32_t *hMax = static_cast<uint32_t *>(pinned_get(h, 5, 64));
+    if (!dMax || !counts || !hMax) return fail(h, SJBG_E_NOMEM, "sort buffers");
+    SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
+    SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
+                      nseg, dMax));
+    SJBG_CK(h, cudaMemcpyAsync(hMax, dMax, 8, cudaMemcpyDeviceToHost, h->stream));
+    SJBG_CK(h, cudaStreamSynchronize(h->stream));
+    const uint32_t maxk = hMax[0];
+    uint32_t bits = 0;
+    while (bits < 32 && (maxk >> bits)) bits++;
+    const uint32_t passes = (bits + 7) / 8;
+    const size_t smem = sizeof(DownSmem);
+    allow_big_smem(rs_downsweep_kernel, smem);
+    uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
+    for (uint32_t p = 0; p < passes; p++) {
+        const uint32_t shift = 8 * p;
+        SJBG_CK(h, launch(h, "rs_upsweep", rs_upsweep_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)kin,
+                          dSegs, nseg, shift, counts));
+        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs));
+        SJBG_CK(h, launch(h, "rs_downsweep", rs_downsweep_kernel, dim3(plan.tiles), dim3(kSortThreads), smem,
+                          (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, nseg, shift,
+                          (const uint32_t *)counts, dMax + 4));
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    if (kin != keys) {   // odd number of passes: bring the result home
+        SJBG_CK(h, cudaMemcpyAsync(keys, kin, sizeof(uint32_t) * plan.elems, cudaMemcpyDeviceToDevice, h->stream));
+        SJBG_CK(h, cudaMemcpyAsync(vals, vin, sizeof(uint32_t) * plan.elems, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    return SJBG_OK;
+}
+
+int segmented_fr_prefix(sjbg_handle *h, const SortPlan &plan, uint32_t nseg, const SortSeg *dSegs,
+                        const uint32_t *vals, unsigned long long *out) {
+    if (nseg == 0) return SJBG_OK;
+    // the first nseg segments: their tiles are [0, tile0 of segment nseg)
+    const uint32_t tiles = nseg < plan.segs.size() ? plan.segs[nseg].tile0 : plan.tiles;
+    unsigned long long *tsum = static_cast<unsigned long long *>(ws_get(h, WS_AUX3, sizeof(unsigned long long) * tiles));
+    if (!tsum) return fail(h, SJBG_E_NOMEM, "prefix buffers");
+    SJBG_CK(h, launch(h, "fr_tile_sum", fr_tile_sum_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, nseg, tsum));
+    SJBG_CK(h, launch(h, "fr_seg_scan", fr_seg_scan_kernel, dim3(nseg), dim3(32), 0, tsum, dSegs));
+    SJBG_CK(h, launch(h, "fr_tile_scan", fr_tile_scan_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, nseg,
+                      (const unsigned long long *)tsum, out));
+    return SJBG_OK;
+}
+
+}  // namespace sjbg

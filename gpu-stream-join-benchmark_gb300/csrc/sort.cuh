@@ -1,0 +1,60 @@
+// sort.cuh - segmented LSD radix sort of (key, val) pairs and segmented scans
+// (device building blocks of the sort-merge join).
+#pragma once
+
+#include <vector>
+
+#include "runtime.h"
+
+namespace sjbg {
+
+constexpr uint32_t kSortTile = 4096;   // elements per sort tile (16 KB of keys)
+
+// One segment (window side) of the SoA key/val arrays.  A segment occupies
+// [off, off + round_up(n + 1, kSortTile)) so every tile is a whole 16 KB block
+// and position off + n exists (the end of a prefix-sum array).
+struct SortSeg {
+    uint64_t off;     // first element (multiple of kSortTile)
+    uint64_t src;     // first tuple of the segment in the AoS input
+    uint32_t n;       // valid elements
+    uint32_t tile0;   // first tile of this segment in the batch
+    uint32_t ntiles;  // tiles of this segment
+    uint32_t pad;
+};
+
+struct SortPlan {
+    std::vector<SortSeg> segs;
+    uint32_t tiles = 0;
+    uint64_t elems = 0;   // padded total
+};
+
+// Plan segments of lengths n[0..k) read from AoS offsets src[0..k): padded
+// offsets and tile ranges.
+SortPlan sort_plan(const uint64_t *n, const uint64_t *src, uint32_t k);
+
+// AoS tuples -> SoA keys/vals for every segment; segments [0, split) read
+// srcA, the others srcB.
+int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB, uint32_t split, const SortPlan &plan,
+                 const SortSeg *dSegs, uint32_t *keys, uint32_t *vals);
+
+__device__ __forceinline__ uint32_t find_seg(const SortSeg *segs, uint32_t nseg, uint32_t tile) {
+    uint32_t lo = 0, hi = nseg;   // largest s with segs[s].tile0 <= tile
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (segs[mid].tile0 <= tile) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Stable LSD sort of every segment by key; keys/vals hold the input and the
+// sorted result on return (keys2/vals2 are scratch).  Passes = ceil(bits/8)
+// where bits covers the largest key (read back once).
+int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
+                        uint32_t *keys2, uint32_t *vals2);
+
+// Exclusive prefix sums of fr(val) (u64, mod 2^64) of the first nseg
+// segments into out (same padded layout; positions 0..n of each segment).
+int segmented_fr_prefix(sjbg_handle *h, const SortPlan &plan, uint32_t nseg, const SortSeg *dSegs,
+                        const uint32_t *vals, unsigned long long *out);
+
+}  // namespace sjbg

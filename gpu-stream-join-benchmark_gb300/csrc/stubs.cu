@@ -2,8 +2,6 @@
 #include "stream.cuh"
 namespace sjbg {
 int eager_init(sjbg_handle *h) { return fail(h, SJBG_E_UNSUPPORTED, "eager not built yet"); }
-int nlj_lazy_batch(sjbg_handle *h, const sjbg_tuple *, const sjbg_tuple *, const WinHost *, uint32_t, sjbg_pair *, WinAcc *, bool) { return fail(h, SJBG_E_UNSUPPORTED, "nlj not built"); }
-int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *, const sjbg_tuple *, const WinHost *, uint32_t, sjbg_pair *, WinAcc *, bool) { return fail(h, SJBG_E_UNSUPPORTED, "smj not built"); }
 }
 using namespace sjbg;
 extern "C" {
