@@ -1,10 +1,40 @@
-// eager.cuh - eager (per-batch) executors.
+// eager.cuh - eager (per-batch) executors: state layout.
 #pragma once
 #include "runtime.h"
 
 namespace sjbg {
-struct EagerState {
-    int placeholder = 0;
+
+constexpr uint32_t kEagerMaxSortBatch = 8192;   // eager sort-merge batches are sorted by one CTA
+
+// One side's state of the current eager window (device memory).
+struct EagerSide {
+    sjbg_tuple *tuples = nullptr;   // arrival order, cap tuples
+    uint64_t n = 0;                 // tuples so far in this window
+    // hash join: open-addressing table keyed by key, with per-key chains
+    uint32_t *tkeys = nullptr;      // slots + 1 (last slot: key 0xFFFFFFFF)
+    uint32_t *tcnt = nullptr;
+    unsigned long long *tsum = nullptr;   // sum of this side's pair hash (left: fr, right: gs)
+    uint32_t *thead = nullptr;
+    uint32_t *next = nullptr;       // chain link per tuple (index into tuples)
+    // sort-merge join: the side's tuples sorted by key, plus prefix sums of its pair hash
+    uint32_t *skeys = nullptr, *svals = nullptr;
+    uint32_t *skeys2 = nullptr, *svals2 = nullptr;
+    unsigned long long *F = nullptr;   // n + 1 entries
 };
+
+struct EagerState {
+    EagerSide side[2];
+    uint64_t cap = 0;          // tuples per side
+    uint32_t table_bits = 0;
+    WinAcc *acc = nullptr;     // current window totals (device)
+    unsigned long long *batch_count = nullptr;   // device slot for the last batch's matches
+    sjbg_pair *pairs = nullptr;   // current window's pairs (device), pairs_cap entries
+    uint64_t pairs_cap = 0;
+    uint32_t *sort_tmp = nullptr;  // sorted incoming batch: keys then vals (2 * kEagerMaxSortBatch)
+    std::vector<void *> allocs;
+    ~EagerState();
+};
+
 int eager_init(sjbg_handle *h);
+
 }  // namespace sjbg

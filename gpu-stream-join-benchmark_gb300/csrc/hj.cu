@@ -35,6 +35,7 @@
 namespace sjbg {
 
 constexpr int kTile = 4096;          // tuples per partitioning tile
+constexpr uint32_t kHistTiles = 16;  // tiles per histogram CTA (amortises its set-up)
 constexpr int kPartThreads = 512;
 constexpr int kJoinThreads = 512;
 constexpr uint32_t kMaxBucketsLog2 = 14;
@@ -98,24 +99,25 @@ __device__ __forceinline__ bool warp_group(bool valid, uint32_t tag, unsigned lo
 __global__ void __launch_bounds__(kPartThreads)
 part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                  uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                 const uint32_t *__restrict__ hgroupL, const uint32_t *__restrict__ hgroupR,
                  uint32_t *__restrict__ cnt, uint32_t B, const LearnedModel *__restrict__ models,
                  HeavyAcc *__restrict__ hacc) {
     extern __shared__ uint32_t hist[];
     __shared__ HeavySet hs;
     __shared__ uint32_t hcnt[kMaxHeavy];
     __shared__ unsigned long long hsum[kMaxHeavy];
-    const uint32_t tilesL = tileL[nwin];
-    const bool right = blockIdx.x >= tilesL;
-    const uint32_t t = right ? blockIdx.x - tilesL : blockIdx.x;
+    // this CTA covers tiles [t, t + kHistTiles) of one window side ("hist groups")
+    const bool right = blockIdx.x >= hgroupL[nwin];
+    const uint32_t g = right ? blockIdx.x - hgroupL[nwin] : blockIdx.x;
+    const uint32_t *hp = right ? hgroupR : hgroupL;
     const uint32_t *tp = right ? tileR : tileL;
-    const uint32_t w = find_window(tp, nwin, t);
+    const uint32_t w = find_window(hp, nwin, g);
     const WinPlan wp = wins[w];
     const Classifier cls = make_classifier(wp, models);
     const bool heavy = cls.m && cls.m->n_heavy;
     const uint64_t nside = right ? wp.n_right : wp.n_left;
-    const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
-    const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
-    const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
+    const uint32_t t_first = (g - hp[w]) * kHistTiles;            // tile index inside the window
+    const uint32_t t_end = min(t_first + kHistTiles, tp[w + 1] - tp[w]);
     const uint32_t P = 1u << wp.log2_buckets;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
     if (heavy) {
@@ -123,18 +125,22 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         heavy_set_load(hs, cls.m);   // ends with a barrier
     }
     __syncthreads();
+    // the hottest heavy keys (the fit orders heavy keys by sampled count) are
+    // accumulated in registers; other heavy keys with shared atomics
+    constexpr int kRegHeavy = 4;
+    uint32_t rc[kRegHeavy] = {0, 0, 0, 0};
+    unsigned long long rs[kRegHeavy] = {0, 0, 0, 0};
     constexpr int kPer = kTile / kPartThreads;
+    for (uint32_t tt = t_first; tt < t_end; tt++) {
+    const uint64_t start = (uint64_t)tt * kTile;
+    const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+    const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
     uint4 v[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; k++) {   // all of the thread's loads in flight before any use
         const uint32_t i = threadIdx.x + k * kPartThreads;
         v[k] = i < n ? __ldg(src + i) : make_uint4(0u, 0u, 0u, 0u);   // whole 16-byte tuple
     }
-    // the hottest heavy keys (the fit orders heavy keys by sampled count) are
-    // accumulated in registers; other heavy keys with shared atomics
-    constexpr int kRegHeavy = 4;
-    uint32_t rc[kRegHeavy] = {0, 0, 0, 0};
-    unsigned long long rs[kRegHeavy] = {0, 0, 0, 0};
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
         const uint32_t i = threadIdx.x + k * kPartThreads;
@@ -163,6 +169,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const uint32_t b = valid ? cls.bucket(key) : 0u;
             if (warp_group(valid, b, 0ull, false, &gs, &gsum)) atomicAdd(&hist[b], gs);
         }
+    }
     }
     if (heavy) {
 #pragma unroll
@@ -640,7 +647,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     // ---- plan
     std::vector<WinPlan> plan(n);
-    std::vector<uint32_t> tileL(n + 1), tileR(n + 1);
+    std::vector<uint32_t> tileL(n + 1), tileR(n + 1), hgL(n + 1), hgR(n + 1);
     uint64_t B = 0, totL = 0, totR = 0;
     uint32_t maxP = 1;
     for (uint32_t w = 0; w < n; w++) {
@@ -661,6 +668,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         maxP = std::max(maxP, 1u << lg);
         tileL[w + 1] = tileL[w] + (uint32_t)((wh.n_left + kTile - 1) / kTile);
         tileR[w + 1] = tileR[w] + (uint32_t)((wh.n_right + kTile - 1) / kTile);
+        hgL[w + 1] = hgL[w] + (tileL[w + 1] - tileL[w] + kHistTiles - 1) / kHistTiles;
+        hgR[w + 1] = hgR[w] + (tileR[w + 1] - tileR[w] + kHistTiles - 1) / kHistTiles;
         totL += wh.n_left;
         totR += wh.n_right;
     }
@@ -672,19 +681,23 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     // ---- upload plan, tile prefixes and bucket->window map in one copy
     const size_t planB = sizeof(WinPlan) * n, tileB = sizeof(uint32_t) * (n + 1), bwB = sizeof(uint32_t) * B;
-    const size_t upB = planB + 2 * tileB + bwB;
+    const size_t upB = planB + 4 * tileB + bwB;
     uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 0, upB));
     uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_WIN_PLAN, upB));
     if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "plan buffers");
     std::memcpy(hst, plan.data(), planB);
     std::memcpy(hst + planB, tileL.data(), tileB);
     std::memcpy(hst + planB + tileB, tileR.data(), tileB);
-    std::memcpy(hst + planB + 2 * tileB, bwin.data(), bwB);
+    std::memcpy(hst + planB + 2 * tileB, hgL.data(), tileB);
+    std::memcpy(hst + planB + 3 * tileB, hgR.data(), tileB);
+    std::memcpy(hst + planB + 4 * tileB, bwin.data(), bwB);
     SJBG_CK(h, cudaMemcpyAsync(dev, hst, upB, cudaMemcpyHostToDevice, h->stream));
     WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
     const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
     const uint32_t *dTileR = reinterpret_cast<const uint32_t *>(dev + planB + tileB);
-    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 2 * tileB);
+    const uint32_t *dHgL = reinterpret_cast<const uint32_t *>(dev + planB + 2 * tileB);
+    const uint32_t *dHgR = reinterpret_cast<const uint32_t *>(dev + planB + 3 * tileB);
+    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 4 * tileB);
 
     uint32_t *dCnt = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CNT, sizeof(uint32_t) * 2 * B));
     uint32_t *dStart = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_START, sizeof(uint32_t) * 2 * B));
@@ -706,8 +719,9 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
     const uint32_t tiles = tileL[n] + tileR[n];
     if (tiles) {
-        SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(tiles), dim3(kPartThreads), sizeof(uint32_t) * maxP,
-                          dL, dR, dPlan, n, dTileL, dTileR, dCnt, (uint32_t)B, dModels, dHeavy));
+        SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(hgL[n] + hgR[n]), dim3(kPartThreads),
+                          sizeof(uint32_t) * maxP, dL, dR, dPlan, n, dTileL, dTileR, dHgL, dHgR, dCnt, (uint32_t)B,
+                          dModels, dHeavy));
         if (learned)
             SJBG_CK(h, launch(h, "heavy_finish", heavy_finish_kernel, dim3(n), dim3(256), 0, (const WinPlan *)dPlan, n,
                               dModels, (const HeavyAcc *)dHeavy, acc));

@@ -35,24 +35,22 @@ struct NljItem {
     uint32_t win, l0, r0, pad;
 };
 
+// One CTA's share of a window: left tuples [l0, l0 + kLTile) against right
+// tuples [r0, r0 + kRSplit).  Adds count/xor/prod to *acc (and the count to
+// *extra_count when given); pairs go to pout[0, pcap) via *npairs.
 template <bool kEnum, bool kPairs>
-__global__ void __launch_bounds__(kNljThreads)
-nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
-           const NljItem *__restrict__ items, WinAcc *__restrict__ acc, sjbg_pair *__restrict__ pairs) {
+__device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uint32_t nL,
+                                          const sjbg_tuple *__restrict__ Rw, uint32_t nR, uint32_t l0, uint32_t r0,
+                                          WinAcc *acc, unsigned long long *extra_count, sjbg_pair *pout,
+                                          uint64_t pcap) {
     __shared__ __align__(16) uint32_t rkeys[kChunk];
     __shared__ __align__(16) uint32_t rvals[kChunk];
-    const NljItem it = items[blockIdx.x];
-    const WinPlan wp = wins[it.win];
-    const sjbg_tuple *Lw = L + wp.left_off;
-    const sjbg_tuple *Rw = R + wp.right_off;
-    const uint32_t nL = (uint32_t)wp.n_left, nR = (uint32_t)wp.n_right;
-
     uint32_t lk[kLReg], lv[kLReg];
     uint32_t lvalid = 0;
     uint32_t fill = 0;
 #pragma unroll
     for (int a = 0; a < kLReg; a++) {
-        const uint32_t li = it.l0 + a * kNljThreads + threadIdx.x;
+        const uint32_t li = l0 + a * kNljThreads + threadIdx.x;
         if (li < nL) {
             const uint2 t = __ldg(reinterpret_cast<const uint2 *>(Lw + li));
             lk[a] = t.x;
@@ -66,11 +64,8 @@ nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, c
         if (!((lvalid >> a) & 1u)) { lk[a] = fill; lv[a] = 0; }   // invalid slots only cause false alarms
 
     unsigned long long count = 0, xr = 0, prod = 0;
-    const uint32_t r_end = min(nR, it.r0 + kRSplit);
-    const uint64_t pcap = kPairs ? wp.pairs_cap : 0;
-    sjbg_pair *pout = kPairs ? pairs + wp.pairs_off : nullptr;
-
-    for (uint32_t c0 = it.r0; c0 < r_end; c0 += kChunk) {
+    const uint32_t r_end = min(nR, r0 + kRSplit);
+    for (uint32_t c0 = r0; c0 < r_end; c0 += kChunk) {
         const uint32_t m = min(kChunk, r_end - c0);
         const uint32_t mpad = (m + kVote - 1) / kVote * kVote;
         __syncthreads();
@@ -116,7 +111,7 @@ nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, c
                 uint32_t tot;
                 const uint32_t ex = warp_excl_scan(mine, &tot);
                 unsigned long long base = 0;
-                if (lane_id() == 0 && tot) base = atomicAdd(&acc[it.win].npairs, (unsigned long long)tot);
+                if (lane_id() == 0 && tot) base = atomicAdd(&acc->npairs, (unsigned long long)tot);
                 base = __shfl_sync(0xFFFFFFFFu, base, 0) + ex;
                 for (uint32_t q = r; q < qe && mine; q++) {
                     const uint32_t k = rkeys[q];
@@ -131,7 +126,47 @@ nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, c
             }
         }
     }
-    flush_acc(&acc[it.win], count, xr, prod);
+    flush_acc(acc, count, xr, prod);
+    if (extra_count) {
+        const unsigned long long c = warp_sum_u64(count);
+        if (lane_id() == 0 && c) atomicAdd(extra_count, c);
+    }
+}
+
+template <bool kEnum, bool kPairs>
+__global__ void __launch_bounds__(kNljThreads)
+nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
+           const NljItem *__restrict__ items, WinAcc *__restrict__ acc, sjbg_pair *__restrict__ pairs) {
+    const NljItem it = items[blockIdx.x];
+    const WinPlan wp = wins[it.win];
+    nlj_block<kEnum, kPairs>(L + wp.left_off, (uint32_t)wp.n_left, R + wp.right_off, (uint32_t)wp.n_right, it.l0, it.r0,
+                             &acc[it.win], nullptr, kPairs ? pairs + wp.pairs_off : nullptr, kPairs ? wp.pairs_cap : 0);
+}
+
+// Eager form: one window given by scalar arguments (no uploaded plan, so it
+// can be captured in a CUDA graph); blockIdx.x = left tile, blockIdx.y = right split.
+template <bool kEnum, bool kPairs>
+__global__ void __launch_bounds__(kNljThreads)
+nlj_pair_kernel(const sjbg_tuple *__restrict__ L, uint32_t nL, const sjbg_tuple *__restrict__ R, uint32_t nR,
+                WinAcc *acc, unsigned long long *batch_count, sjbg_pair *pairs, uint64_t pairs_cap) {
+    nlj_block<kEnum, kPairs>(L, nL, R, nR, blockIdx.x * kLTile, blockIdx.y * kRSplit, acc, batch_count, pairs,
+                             pairs_cap);
+}
+
+int nlj_pair_launch(sjbg_handle *h, const sjbg_tuple *L, uint64_t nL, const sjbg_tuple *R, uint64_t nR, WinAcc *acc,
+                    unsigned long long *batch_count, sjbg_pair *pairs, uint64_t pairs_cap, bool enumerate) {
+    if (nL == 0 || nR == 0) return SJBG_OK;
+    const dim3 grid((uint32_t)((nL + kLTile - 1) / kLTile), (uint32_t)((nR + kRSplit - 1) / kRSplit));
+    if (pairs)
+        SJBG_CK(h, launch(h, "eager_nlj_pairs", nlj_pair_kernel<true, true>, grid, dim3(kNljThreads), 0, L,
+                          (uint32_t)nL, R, (uint32_t)nR, acc, batch_count, pairs, pairs_cap));
+    else if (enumerate)
+        SJBG_CK(h, launch(h, "eager_nlj_xor", nlj_pair_kernel<true, false>, grid, dim3(kNljThreads), 0, L,
+                          (uint32_t)nL, R, (uint32_t)nR, acc, batch_count, pairs, pairs_cap));
+    else
+        SJBG_CK(h, launch(h, "eager_nlj_count", nlj_pair_kernel<false, false>, grid, dim3(kNljThreads), 0, L,
+                          (uint32_t)nL, R, (uint32_t)nR, acc, batch_count, pairs, pairs_cap));
+    return SJBG_OK;
 }
 
 int nlj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
