@@ -286,7 +286,7 @@ int sjbg_create(const sjbg_config *cfg, sjbg_handle **out) {
         return fail(nullptr, SJBG_E_CUDA, cudaGetErrorString(e));
     h->stream = h->own_stream;
     if (cfg->progressiveness == SJBG_EAGER) {
-        int rc = eager_init(h.get());
+        int rc = eager_init_and_clear(h.get());
         if (rc) {
             std::lock_guard<std::mutex> g(g_err_mu);
             g_create_err = h->err;

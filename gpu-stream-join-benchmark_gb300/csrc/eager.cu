@@ -87,7 +87,7 @@ __device__ __forceinline__ void flush_batch(WinAcc *acc, unsigned long long *bco
 template <bool kEnum, bool kPairs>
 __global__ void __launch_bounds__(256)
 eager_hj_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32_t base, int side, ETab own, ETab oth,
-                const sjbg_tuple *__restrict__ oth_tuples, WinAcc *acc, unsigned long long *bcount,
+                const sjbg_tuple *__restrict__ oth_tuples, uint32_t oth_n, WinAcc *acc, unsigned long long *bcount,
                 sjbg_pair *__restrict__ pairs, uint64_t pcap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
@@ -109,8 +109,10 @@ eager_hj_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32_t base,
             head = oth.head[s];
         }
     }
+    // chains hold indices of the other side's tuples; walks stop at its size
     if (kEnum) {
-        for (uint32_t j = head; j != kNilIdx; j = oth.next[j]) {
+        uint32_t steps = 0;
+        for (uint32_t j = head; j < oth_n && steps < oth_n; j = oth.next[j], steps++) {
             const uint32_t ov = oth_tuples[j].val;
             xr ^= side == 0 ? sjbg_pair_hash(val, ov) : sjbg_pair_hash(ov, val);
         }
@@ -121,7 +123,8 @@ eager_hj_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32_t base,
         unsigned long long b = 0;
         if (lane_id() == 0 && tot) b = atomicAdd(&acc->npairs, (unsigned long long)tot);
         b = __shfl_sync(0xFFFFFFFFu, b, 0) + ex;
-        for (uint32_t j = head; j != kNilIdx; j = oth.next[j], b++) {
+        uint32_t steps = 0;
+        for (uint32_t j = head; j < oth_n && steps < oth_n; j = oth.next[j], b++, steps++) {
             const uint32_t ov = oth_tuples[j].val;
             if (b < pcap) pairs[b] = side == 0 ? sjbg_pair{val, ov} : sjbg_pair{ov, val};
         }
@@ -356,6 +359,18 @@ int eager_init(sjbg_handle *h) {
     return SJBG_OK;
 }
 
+static int eager_clear(sjbg_handle *h);
+
+// Allocate and clear (fresh device memory holds no valid table, run or total).
+int eager_init_and_clear(sjbg_handle *h) {
+    int rc = eager_init(h);
+    if (rc) return rc;
+    rc = eager_clear(h);
+    if (rc) return rc;
+    SJBG_CK(h, cudaStreamSynchronize(h->stream));
+    return SJBG_OK;
+}
+
 static bool eager_enumerates(const sjbg_handle *h) {
     return h->cfg.result_mode != SJBG_RESULT_NO_OUTPUT || (h->cfg.flags & SJBG_F_XOR);
 }
@@ -411,15 +426,18 @@ static int eager_enqueue(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, in
             if (pairs)
                 SJBG_CK(h, launch(h, "eager_hj_pairs", eager_hj_kernel<true, true>, dim3(blocks), dim3(256), 0,
                                   (const sjbg_tuple *)dst, (uint32_t)n, (uint32_t)S.n, side, own, oth,
-                                  (const sjbg_tuple *)O.tuples, st.acc, count_slot, pairs, st.pairs_cap));
+                                  (const sjbg_tuple *)O.tuples, (uint32_t)O.n, st.acc, count_slot, pairs,
+                                  st.pairs_cap));
             else if (en)
                 SJBG_CK(h, launch(h, "eager_hj_xor", eager_hj_kernel<true, false>, dim3(blocks), dim3(256), 0,
                                   (const sjbg_tuple *)dst, (uint32_t)n, (uint32_t)S.n, side, own, oth,
-                                  (const sjbg_tuple *)O.tuples, st.acc, count_slot, pairs, st.pairs_cap));
+                                  (const sjbg_tuple *)O.tuples, (uint32_t)O.n, st.acc, count_slot, pairs,
+                                  st.pairs_cap));
             else
                 SJBG_CK(h, launch(h, "eager_hj_count", eager_hj_kernel<false, false>, dim3(blocks), dim3(256), 0,
                                   (const sjbg_tuple *)dst, (uint32_t)n, (uint32_t)S.n, side, own, oth,
-                                  (const sjbg_tuple *)O.tuples, st.acc, count_slot, pairs, st.pairs_cap));
+                                  (const sjbg_tuple *)O.tuples, (uint32_t)O.n, st.acc, count_slot, pairs,
+                                  st.pairs_cap));
             break;
         }
         case SJBG_ALG_SMJ: {

@@ -36,5 +36,6 @@ struct EagerState {
 };
 
 int eager_init(sjbg_handle *h);
+int eager_init_and_clear(sjbg_handle *h);
 
 }  // namespace sjbg
