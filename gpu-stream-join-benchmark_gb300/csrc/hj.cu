@@ -748,4 +748,95 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     return SJBG_OK;
 }
 
+
+// ------------------------------------------------------------------ caller-provided scratch
+// One window, count mode, radix partitioning, every buffer carved out of the
+// caller-provided device scratch `sc` (no allocation, no host-to-device copy:
+// the plan is written by a set-up kernel).  Used by the allocation-free entry
+// point in noalloc.cu.
+struct RawScratch {
+    WinPlan plan;
+    uint32_t tile[8];   // tileL {0, tL}, tileR {0, tR}, hgL {0, gL}, hgR {0, gR}
+    WinAcc acc;
+};
+
+__global__ void raw_setup_kernel(RawScratch *rs, uint32_t *bucket_win, uint32_t *cnt, uint32_t P, uint64_t nL,
+                                 uint64_t nR, uint32_t lg, uint32_t tL, uint32_t tR) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        WinPlan &p = rs->plan;
+        p.left_off = 0; p.n_left = nL; p.right_off = 0; p.n_right = nR;
+        p.pairs_off = 0; p.pairs_cap = 0;
+        p.bucket_base = 0; p.log2_buckets = lg; p.model = 0xFFFFFFFFu; p.pad = 0;
+        rs->tile[0] = 0; rs->tile[1] = tL;
+        rs->tile[2] = 0; rs->tile[3] = tR;
+        rs->tile[4] = 0; rs->tile[5] = (tL + kHistTiles - 1) / kHistTiles;
+        rs->tile[6] = 0; rs->tile[7] = (tR + kHistTiles - 1) / kHistTiles;
+        rs->acc = WinAcc{0, 0, 0, 0, 0};
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * P; i += gridDim.x * blockDim.x) {
+        cnt[i] = 0;
+        if (i < P) bucket_win[i] = 0;
+    }
+}
+
+__global__ void raw_finish_kernel(const RawScratch *rs, sjbg_window_result *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        sjbg_window_result r;
+        r.count = rs->acc.count;
+        r.xor_checksum = 0;
+        r.prod_checksum = rs->acc.prod;
+        r.n_pairs = 0;
+        r.status = SJBG_OK;
+        r.flags = 0;
+        r.partitioner_used = SJBG_PART_RADIX;
+        r.ms = 0.0f;
+        *out = r;
+    }
+}
+
+size_t hj_raw_scratch_bytes(uint64_t max_tuples) {
+    const uint64_t P = (max_tuples + 4095) / 4096;
+    return 256 * 4 + sizeof(RawScratch) + 256 + 4 * 4 * P + 256 + 2 * 8 * max_tuples + 1024;
+}
+
+static uint8_t *align256(uint8_t *p) { return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255)); }
+
+int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR, uint64_t nR, uint8_t *sc,
+                        size_t sc_bytes, sjbg_window_result *dOut, cudaStream_t st) {
+    uint32_t lg = 0;
+    while (((uint64_t)4096 << lg) < nL) lg++;
+    if (nL == 0 || nR == 0) lg = 0;
+    const uint32_t P = 1u << lg;
+    const uint32_t tL = (uint32_t)((nL + kTile - 1) / kTile), tR = (uint32_t)((nR + kTile - 1) / kTile);
+    uint8_t *p = align256(sc);
+    RawScratch *rs = reinterpret_cast<RawScratch *>(p);
+    p = align256(p + sizeof(RawScratch));
+    uint32_t *bwin = reinterpret_cast<uint32_t *>(p);
+    uint32_t *cnt = bwin + P;
+    uint32_t *start = cnt + 2 * P;
+    uint32_t *cur = start + 2 * P;
+    p = align256(reinterpret_cast<uint8_t *>(cur + 2 * P));
+    uint64_t *pL = reinterpret_cast<uint64_t *>(p);
+    uint64_t *pR = pL + std::max<uint64_t>(nL, 1);
+    if (reinterpret_cast<uint8_t *>(pR + std::max<uint64_t>(nR, 1)) > sc + sc_bytes) return SJBG_E_CAPACITY;
+    raw_setup_kernel<<<4, 256, 0, st>>>(rs, bwin, cnt, P, nL, nR, lg, tL, tR);
+    const uint32_t *tl = rs->tile;
+    if (tL + tR) {
+        const uint32_t groups = (tL + kHistTiles - 1) / kHistTiles + (tR + kHistTiles - 1) / kHistTiles;
+        part_hist_kernel<<<groups, kPartThreads, sizeof(uint32_t) * P, st>>>(
+            dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr);
+        part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);
+        const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * P;
+        allow_big_smem(part_scatter_kernel, scatterSmem);
+        part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, cur, P, pL,
+                                                                          pR, nullptr);
+        const uint32_t bits = 13;
+        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
+        allow_big_smem(bucket_join_count_kernel, smem);
+        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, bits);
+    }
+    raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);
+    return cudaGetLastError() == cudaSuccess ? SJBG_OK : SJBG_E_CUDA;
+}
+
 }  // namespace sjbg

@@ -40,6 +40,7 @@ EXPORTS = [
     "sjbg_eager_execute", "sjbg_eager_clear_states", "sjbg_eager_window_result", "sjbg_eager_end_of_stream",
     "sjbg_eager_run", "sjbg_stream_open", "sjbg_stream_push", "sjbg_stream_poll", "sjbg_stream_close",
     "sjbg_generate", "sjbg_kernel_stats", "sjbg_kernel_stats_reset", "sjbg_launch_count",
+    "sjbg_lazy_hj_noalloc",
 ]
 
 
@@ -114,6 +115,7 @@ def load(path: str = LIB_PATH):
         L.sjbg_kernel_stats_reset.argtypes = [vp]
         L.sjbg_launch_count.argtypes = [vp]
         L.sjbg_launch_count.restype = u64
+        L.sjbg_lazy_hj_noalloc.argtypes = [vp, u64, vp, u64, vp, vp]
         _lib = L
     return _lib
 
@@ -136,6 +138,16 @@ def _len(a, dtype=TUPLE_DTYPE) -> int:
     if hasattr(a, "numel") and hasattr(a, "element_size"):
         return a.numel() * a.element_size() // dtype.itemsize
     raise TypeError("length of a device buffer must be given explicitly")
+
+
+def lazy_hj_noalloc(left_dev_ptr: int, n_left: int, right_dev_ptr: int, n_right: int, out_dev_ptr: int,
+                    stream: int | None = None) -> None:
+    """The allocation-free lazy hash join (device inputs, device result record)."""
+    L = load()
+    rc = L.sjbg_lazy_hj_noalloc(C.c_void_p(left_dev_ptr), n_left, C.c_void_p(right_dev_ptr), n_right,
+                                C.c_void_p(out_dev_ptr), C.c_void_p(stream) if stream else None)
+    if rc:
+        raise SjbgError(rc, L.sjbg_last_error(None).decode())
 
 
 class Joiner:

@@ -266,6 +266,22 @@ SJBG_API int sjbg_stream_close(sjbg_handle *h, sjbg_stream_stats *stats);
 SJBG_API int sjbg_generate(sjbg_handle *h, sjbg_tuple *dev_out, uint64_t first, uint64_t n,
                   uint64_t seed, uint64_t domain, const uint64_t *zipf_table, uint64_t perm_seed);
 
+/* ---- allocation-free lazy hash join ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (a host framework that owns every device allocation, or a
+ * steady-state loop that must not allocate): the lazy hash join of one window
+ * (count and prod_checksum; radix partitioning) that allocates nothing and
+ * copies nothing from the host.  left/right (n_left, n_right <= 2^20 tuples,
+ * else SJBG_E_CAPACITY) and out are DEVICE memory; the work is enqueued on
+ * cuda_stream (NULL = the legacy default stream) and out is written when it
+ * completes.  Needs no handle.  Its scratch is a fixed 17 MiB device array
+ * that every GPU loading the library holds until exit; the first call on a
+ * device looks up that array's address and should come before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller. */
+SJBG_API int sjbg_lazy_hj_noalloc(const sjbg_tuple *left, uint64_t n_left, const sjbg_tuple *right,
+                                  uint64_t n_right, sjbg_window_result *out, void *cuda_stream);
+
 /* ---- kernel profile (SJBG_F_PROFILE) ---------------------------------------------
  * Per kernel name: launches and summed CUDA-event time since the last reset. */
 SJBG_API int sjbg_kernel_stats(sjbg_handle *h, uint32_t index, char *name, size_t name_len,
