@@ -19,6 +19,11 @@ sjbg_handle::~sjbg_handle() {
     if (device >= 0) cudaSetDevice(device);
     eager.reset();
     streaming.reset();
+    for (auto &g : graphs) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        for (auto &b : g->pinned)
+            if (b.p) cudaFreeHost(b.p);
+    }
     for (auto &b : ws)
         if (b.p) cudaFree(b.p);
     for (auto &b : pinned)
@@ -128,7 +133,7 @@ void profile_collect(sjbg_handle *h) {
 static bool wants_pairs(const sjbg_handle *h) { return h->cfg.result_mode != SJBG_RESULT_NO_OUTPUT; }
 
 // Run windows whose spans index device arrays dL / dR; dPairs (device) may be null.
-static int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                            sjbg_pair *dPairs, WinAcc *hAcc, uint32_t *part_used) {
     const bool pairs = dPairs != nullptr;
     const bool enumerate = pairs || (h->cfg.flags & SJBG_F_XOR);
@@ -170,6 +175,92 @@ static void fill_result(const sjbg_handle *h, const WinAcc &a, const WinHost &w,
     (void)h;
 }
 
+// Batched lazy call on device inputs through a cached CUDA graph: the first
+// call with a given signature runs normally (sizing every workspace), then is
+// captured with private pinned staging buffers; later identical calls replay it.
+static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                      sjbg_pair *dPairs, bool enumerate, sjbg_window_result *out) {
+    std::vector<uint64_t> key = {h->cfg.algorithm, h->cfg.partitioner, h->cfg.flags, h->cfg.result_mode,
+                                 (uint64_t)(uintptr_t)dL, (uint64_t)(uintptr_t)dR, (uint64_t)(uintptr_t)dPairs, n,
+                                 h->tune.bucket_target, (uint64_t)h->tune.persistent_join,
+                                 (uint64_t)(uintptr_t)h->stream};
+    for (uint32_t w = 0; w < n; w++) {
+        const WinHost &x = wins[w];
+        key.insert(key.end(), {x.left_off, x.n_left, x.right_off, x.n_right, x.pairs_off, x.pairs_cap});
+    }
+    sjbg_handle::GraphEntry *entry = nullptr;
+    for (auto &g : h->graphs)
+        if (g->key == key) entry = g.get();
+    cudaEvent_t e0 = event_get(h), e1 = event_get(h);
+    WinAcc *hAcc = nullptr;
+    uint32_t part_used = SJBG_PART_NONE;
+    if (entry) {
+        SJBG_CK(h, cudaEventRecord(e0, h->stream));
+        SJBG_CK(h, cudaGraphLaunch(entry->exec, h->stream));
+        SJBG_CK(h, cudaEventRecord(e1, h->stream));
+        hAcc = static_cast<WinAcc *>(entry->pinned[3].p);
+        part_used = entry->part_used;
+    } else {
+        hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * std::max<uint32_t>(n, 1)));
+        if (!hAcc) return fail(h, SJBG_E_NOMEM, "result staging");
+        SJBG_CK(h, cudaEventRecord(e0, h->stream));
+        int rc = run_lazy_device(h, dL, dR, wins, n, dPairs, hAcc, &part_used);   // warm-up: sizes every buffer
+        if (rc) return rc;
+        SJBG_CK(h, cudaEventRecord(e1, h->stream));
+        SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        profile_collect(h);
+        auto e = std::make_unique<sjbg_handle::GraphEntry>();
+        e->key = key;
+        e->part_used = part_used;
+        for (int i = 0; i < 6; i++) {   // private copies of the staging buffers the capture will reference
+            if (!h->pinned[i].bytes) continue;
+            if (cudaMallocHost(&e->pinned[i].p, h->pinned[i].bytes) != cudaSuccess) {
+                cudaGetLastError();
+                for (auto &b : e->pinned)
+                    if (b.p) cudaFreeHost(b.p);
+                return fail(h, SJBG_E_NOMEM, "graph staging");
+            }
+            e->pinned[i].bytes = h->pinned[i].bytes;
+        }
+        for (int i = 0; i < 6; i++) std::swap(h->pinned[i], e->pinned[i]);
+        h->capturing = true;
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed);
+        uint32_t pu2 = 0;
+        int rc2 = ce == cudaSuccess ? run_lazy_device(h, dL, dR, wins, n, dPairs,
+                                                      static_cast<WinAcc *>(h->pinned[3].p), &pu2)
+                                    : SJBG_E_CUDA;
+        cudaError_t ce2 = cudaStreamEndCapture(h->stream, &graph);
+        h->capturing = false;
+        for (int i = 0; i < 6; i++) std::swap(h->pinned[i], e->pinned[i]);
+        if (rc2 == SJBG_OK && ce == cudaSuccess && ce2 == cudaSuccess && graph) {
+            if (cudaGraphInstantiate(&e->exec, graph, 0) != cudaSuccess) e->exec = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (e->exec) {
+            if (h->graphs.size() >= 8) {
+                auto &old = h->graphs.front();
+                cudaGraphExecDestroy(old->exec);
+                for (auto &b : old->pinned)
+                    if (b.p) cudaFreeHost(b.p);
+                h->graphs.erase(h->graphs.begin());
+            }
+            h->graphs.push_back(std::move(e));
+        } else {
+            for (auto &b : e->pinned)
+                if (b.p) cudaFreeHost(b.p);
+        }
+    }
+    SJBG_CK(h, cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    h->event_pool.push_back(e0);
+    h->event_pool.push_back(e1);
+    for (uint32_t w = 0; w < n; w++) fill_result(h, hAcc[w], wins[w], enumerate, dPairs != nullptr, part_used, ms, &out[w]);
+    return SJBG_OK;
+}
+
 int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32_t mem, const WinHost *wins,
                 uint32_t n, sjbg_pair *pairs, sjbg_window_result *out) {
     if (!h) return SJBG_E_INVALID;
@@ -190,6 +281,14 @@ int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32
     const bool want = wants_pairs(h) && pairs != nullptr && needP > 0;
     const bool enumerate = want || (h->cfg.flags & SJBG_F_XOR);
 
+    if (h->cfg.flags & SJBG_F_AUTOTUNE) {
+        if (mem == SJBG_MEM_DEVICE) {
+            int rc = autotune_lazy(h, L, R, wins, n, enumerate);
+            if (rc) return rc;
+        }
+    }
+    if ((h->cfg.flags & SJBG_F_GRAPH) && mem == SJBG_MEM_DEVICE && h->cfg.result_mode != SJBG_RESULT_COUNT_KERNEL)
+        return lazy_graph(h, L, R, wins, n, want ? pairs : nullptr, enumerate, out);
     cudaEvent_t e0 = event_get(h), e1 = event_get(h);
     SJBG_CK(h, cudaEventRecord(e0, h->stream));
     const sjbg_tuple *dL = L, *dR = R;

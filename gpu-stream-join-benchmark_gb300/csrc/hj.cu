@@ -457,13 +457,13 @@ __device__ __forceinline__ bool agg_insert(const CountTable &t, bool valid, uint
 
 constexpr int kJoinPer = 8;   // elements per thread per tile (independent loads in flight)
 
-__global__ void __launch_bounds__(kJoinThreads)
-bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
-                         const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
-                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t table_bits) {
+__device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restrict__ partL,
+                                                  const uint64_t *__restrict__ partR,
+                                                  const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt,
+                                                  uint32_t B, const uint32_t *__restrict__ bucket_win,
+                                                  WinAcc *__restrict__ acc, uint32_t table_bits) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t novf;
-    const uint32_t b = blockIdx.x;
     const uint32_t nR = cnt[b], nS = cnt[B + b];
     if (nR == 0 || nS == 0) return;
     uint64_t *Rb = partL + start[b];
@@ -535,13 +535,13 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
 constexpr uint32_t kEnumChunk = 4096;  // left tuples per chained chunk
 constexpr uint32_t kNil = 0xFFFFFFFFu;
 
-__global__ void __launch_bounds__(kJoinThreads)
-bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
-                        const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
-                        const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc,
-                        const WinPlan *__restrict__ wins, sjbg_pair *__restrict__ pairs, uint32_t table_bits) {
+__device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__restrict__ partL,
+                                                 const uint64_t *__restrict__ partR,
+                                                 const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt,
+                                                 uint32_t B, const uint32_t *__restrict__ bucket_win,
+                                                 WinAcc *__restrict__ acc, const WinPlan *__restrict__ wins,
+                                                 sjbg_pair *__restrict__ pairs, uint32_t table_bits) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    const uint32_t b = blockIdx.x;
     const uint32_t nR = cnt[b], nS = cnt[B + b];
     if (nR == 0 || nS == 0) return;
     const uint64_t *Rb = partL + start[b];
@@ -630,6 +630,49 @@ bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__re
     flush_acc(&acc[w], count, xr, prod);
 }
 
+// Bucket joins: one CTA per bucket (queue == nullptr) or persistent CTAs that
+// take buckets from a device work queue (an atomic counter) until it runs dry.
+__global__ void __launch_bounds__(kJoinThreads)
+bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
+                         const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
+                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t table_bits,
+                         uint32_t *queue) {
+    if (!queue) {
+        join_count_bucket(blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc, table_bits);
+        return;
+    }
+    __shared__ uint32_t item_s;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
+        __syncthreads();
+        const uint32_t b = item_s;
+        if (b >= B) break;
+        join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, table_bits);
+    }
+}
+
+__global__ void __launch_bounds__(kJoinThreads)
+bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
+                        const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
+                        const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc,
+                        const WinPlan *__restrict__ wins, sjbg_pair *__restrict__ pairs, uint32_t table_bits,
+                        uint32_t *queue) {
+    if (!queue) {
+        join_enum_bucket(blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs, table_bits);
+        return;
+    }
+    __shared__ uint32_t item_s;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
+        __syncthreads();
+        const uint32_t b = item_s;
+        if (b >= B) break;
+        join_enum_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs, table_bits);
+    }
+}
+
 // ------------------------------------------------------------------ host driver
 static uint32_t ceil_log2(uint64_t x) {
     uint32_t b = 0;
@@ -643,7 +686,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     const uint32_t part = h->cfg.partitioner;
     const bool learned = part == SJBG_PART_LEARNED;
     if (part_used) *part_used = learned ? SJBG_PART_LEARNED : SJBG_PART_RADIX;
-    const uint64_t target = enumerate ? 2048 : 4096;   // left tuples per bucket (autotuner may change)
+    // left tuples per bucket: 2048 when chains are built, else the tuned target
+    const uint64_t target = enumerate ? 2048 : h->tune.bucket_target;
 
     // ---- plan
     std::vector<WinPlan> plan(n);
@@ -732,18 +776,27 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(tiles), dim3(kPartThreads), scatterSmem,
                           dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels));
     }
+    // persistent CTAs draining a work queue of buckets, or one CTA per bucket
+    uint32_t *queue = nullptr;
+    dim3 jgrid((uint32_t)B);
+    if (h->tune.persistent_join && B > (uint64_t)h->num_sms) {
+        queue = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_WIN, 64));
+        if (!queue) return fail(h, SJBG_E_NOMEM, "work queue");
+        SJBG_CK(h, cudaMemsetAsync(queue, 0, 4, h->stream));
+        jgrid = dim3((uint32_t)std::min<uint64_t>(B, (uint64_t)h->num_sms * (enumerate ? 1 : 1)));
+    }
     if (enumerate) {
         const uint32_t bits = 13;   // 8192 slots for chunks of 4096
         const size_t smem = sizeof(uint32_t) * (2 * ((1u << bits) + 1) + 2 * kEnumChunk);
         allow_big_smem(bucket_join_enum_kernel, smem);
-        SJBG_CK(h, launch(h, "bucket_join_enum", bucket_join_enum_kernel, dim3((uint32_t)B), dim3(kJoinThreads), smem,
-                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits));
+        SJBG_CK(h, launch(h, "bucket_join_enum", bucket_join_enum_kernel, jgrid, dim3(kJoinThreads), smem,
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits, queue));
     } else {
         const uint32_t bits = 13;
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
-        SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, dim3((uint32_t)B), dim3(kJoinThreads), smem,
-                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, bits));
+        SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, jgrid, dim3(kJoinThreads), smem,
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, bits, queue));
     }
     return SJBG_OK;
 }
@@ -833,7 +886,7 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         const uint32_t bits = 13;
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
-        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, bits);
+        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, bits, nullptr);
     }
     raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);
     return cudaGetLastError() == cudaSuccess ? SJBG_OK : SJBG_E_CUDA;

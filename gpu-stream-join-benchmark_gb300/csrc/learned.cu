@@ -402,7 +402,7 @@ __global__ void set_model_kernel(WinPlan *plan, uint32_t n) {
 uint32_t learned_log2_buckets(sjbg_handle *h, uint64_t n_left) {
     if (h->cfg.radix_bits) return h->cfg.radix_bits;
     uint32_t b = 0;
-    while (((uint64_t)4096 << b) < n_left) b++;
+    while (((uint64_t)h->tune.bucket_target << b) < n_left) b++;
     return b;
 }
 

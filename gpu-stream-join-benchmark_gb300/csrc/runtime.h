@@ -59,6 +59,24 @@ struct sjbg_handle {
     uint64_t launches = 0;
     bool capturing = false;
 
+    // tunables (the autotuner picks them per workload shape)
+    struct Tune {
+        uint32_t bucket_target = 4096;   // left tuples per hash-join bucket
+        bool persistent_join = true;     // bucket join drains a device work queue
+        float ms = 0.0f;                 // measured time of the chosen setting (autotuner)
+    } tune;
+
+    // captured batched calls (SJBG_F_GRAPH)
+    struct GraphEntry {
+        std::vector<uint64_t> key;
+        cudaGraphExec_t exec = nullptr;
+        sjbg::DevBuf pinned[6];
+        uint32_t part_used = 0;
+    };
+    std::vector<std::unique_ptr<GraphEntry>> graphs;
+    std::map<std::string, Tune> tuned;   // autotuner decisions by workload shape
+    bool tune_loaded = false;
+
     std::unique_ptr<sjbg::EagerState> eager;
     std::unique_ptr<sjbg::StreamState> streaming;
 
@@ -131,5 +149,13 @@ int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
 
 int generate_device(sjbg_handle *h, sjbg_tuple *out, uint64_t first, uint64_t n, uint64_t seed, uint64_t domain,
                     const uint64_t *table, uint64_t perm_seed);
+
+// Autotuner (tune.cu): choose h->tune for this batch shape, measuring the
+// candidates on the batch itself the first time a shape is seen.
+int autotune_lazy(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                  bool enumerate);
+// One device-side lazy batch (no host synchronisation), used by the runtime and the tuner.
+int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                    sjbg_pair *dPairs, WinAcc *hAcc, uint32_t *part_used);
 
 }  // namespace sjbg

@@ -377,12 +377,15 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
     uint32_t *counts = static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * plan.tiles));
     uint32_t *hMax = static_cast<uint32_t *>(pinned_get(h, 5, 64));
     if (!dMax || !counts || !hMax) return fail(h, SJBG_E_NOMEM, "sort buffers");
-    SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
-    SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
-                      nseg, dMax));
-    SJBG_CK(h, cudaMemcpyAsync(hMax, dMax, 8, cudaMemcpyDeviceToHost, h->stream));
-    SJBG_CK(h, cudaStreamSynchronize(h->stream));
-    const uint32_t maxk = hMax[0];
+    uint32_t maxk = 0xFFFFFFFFu;   // under graph capture the key range is not read back: all 4 passes
+    if (!h->capturing) {
+        SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
+        SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys,
+                          dSegs, nseg, dMax));
+        SJBG_CK(h, cudaMemcpyAsync(hMax, dMax, 8, cudaMemcpyDeviceToHost, h->stream));
+        SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        maxk = hMax[0];
+    }
     uint32_t bits = 0;
     while (bits < 32 && (maxk >> bits)) bits++;
     const uint32_t passes = (bits + 7) / 8;

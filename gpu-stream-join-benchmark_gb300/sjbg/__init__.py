@@ -28,7 +28,7 @@ EAGER, LAZY = 0, 1
 RESULT_NO_OUTPUT, RESULT_COUNT_KERNEL, RESULT_ESTIMATED_SELECTIVITY, RESULT_BITMAP, RESULT_ATOMIC = 0, 1, 2, 3, 4
 PART_AUTO, PART_NONE, PART_RADIX, PART_LEARNED = 0, 1, 2, 3
 MEM_HOST, MEM_DEVICE = 0, 1
-F_XOR, F_PROFILE, F_AUTOTUNE, F_VERIFY = 0x1, 0x2, 0x4, 0x8
+F_XOR, F_PROFILE, F_AUTOTUNE, F_VERIFY, F_GRAPH = 0x1, 0x2, 0x4, 0x8, 0x10
 WR_XOR, WR_PAIRS_TRUNCATED, WR_FALLBACK = 0x1, 0x2, 0x4
 
 STATUS = {0: "OK", 1: "E_INVALID", 2: "E_NOMEM", 3: "E_CUDA", 4: "E_TIMEOUT", 5: "E_CAPACITY",

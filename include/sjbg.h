@@ -115,6 +115,7 @@ enum { SJBG_MEM_HOST = 0, SJBG_MEM_DEVICE = 1 };
 #define SJBG_F_PROFILE  0x2u  /* time every kernel launch with CUDA events */
 #define SJBG_F_AUTOTUNE 0x4u  /* pick buckets / tiles / fan-out by measurement */
 #define SJBG_F_VERIFY   0x8u  /* learned partitioning: also run radix and compare */
+#define SJBG_F_GRAPH    0x10u /* capture batched lazy calls on device inputs in a CUDA graph, replay repeats */
 
 /* sjbg_window_result.flags */
 #define SJBG_WR_XOR             0x1u /* xor_checksum is valid */
