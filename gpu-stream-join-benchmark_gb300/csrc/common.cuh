@@ -7,6 +7,15 @@
 #include "../../include/sjbg.h"
 #include "sjbg_gen.h"
 
+// Block barrier that first reconverges the calling warp: loops whose trip
+// count differs between the lanes of a warp (retry loops on shared atomics
+// in particular) must not reach __syncthreads() with the warp diverged.
+#define SJBG_BARRIER()   \
+    do {                 \
+        __syncwarp();    \
+        __syncthreads(); \
+    } while (0)
+
 namespace sjbg {
 
 constexpr uint32_t kEmptyKey = 0xFFFFFFFFu;   // empty slot marker of shared-memory tables

@@ -154,7 +154,7 @@ eager_sort_batch_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32
             sv[i] = ~0ull;
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     for (uint32_t k = 2; k <= P; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
             for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
@@ -165,7 +165,7 @@ eager_sort_batch_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32
                     if (up ? (a > b) : (a < b)) { sv[i] = b; sv[p] = a; }
                 }
             }
-            __syncthreads();
+            SJBG_BARRIER();
         }
     }
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
@@ -255,7 +255,7 @@ eager_prefix_tiles_kernel(const uint32_t *__restrict__ vals, uint32_t n, int sid
         if (base + i < n) acc += own_hash(side, vals[base + i]);
     acc = warp_sum_u64(acc);
     if (lane_id() == 0) ws[warp_id()] = acc;
-    __syncthreads();
+    SJBG_BARRIER();
     if (threadIdx.x == 0) {
         unsigned long long s = 0;
         for (int i = 0; i < 8; i++) s += ws[i];
@@ -290,7 +290,7 @@ eager_prefix_apply_kernel(const uint32_t *__restrict__ vals, uint32_t n, int sid
         if (lane_id() >= (uint32_t)o) x += y;
     }
     if (lane_id() == 31) wsum[warp_id()] = x;
-    __syncthreads();
+    SJBG_BARRIER();
     unsigned long long wofs = 0;
     for (uint32_t w = 0; w < warp_id(); w++) wofs += wsum[w];
     unsigned long long run = tsum[blockIdx.x] + wofs + x - loc;

@@ -124,7 +124,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum[i] = 0; }
         heavy_set_load(hs, cls.m);   // ends with a barrier
     }
-    __syncthreads();
+    SJBG_BARRIER();
     // the hottest heavy keys (the fit orders heavy keys by sampled count) are
     // accumulated in registers; other heavy keys with shared atomics
     constexpr int kRegHeavy = 4;
@@ -182,7 +182,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             }
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
         if (hist[i]) atomicAdd(&dst[i], hist[i]);
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(1024) part_scan_kernel(const uint32_t *__restr
     for (uint32_t side = 0; side < 2; side++) {
         const uint32_t lo = side * B, hi = lo + B;
         if (threadIdx.x == 0) carry_s = 0;
-        __syncthreads();
+        SJBG_BARRIER();
         for (uint32_t base = lo; base < hi; base += chunk) {
             uint32_t v[kItems], s = 0;
 #pragma unroll
@@ -248,13 +248,13 @@ __global__ void __launch_bounds__(1024) part_scan_kernel(const uint32_t *__restr
             uint32_t wt;
             const uint32_t ex = warp_excl_scan(s, &wt);
             if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
-            __syncthreads();
+            SJBG_BARRIER();
             if (warp_id() == 0) {
                 const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0;
                 uint32_t tt;
                 warp_tot[lane_id()] = warp_excl_scan(x, &tt);
             }
-            __syncthreads();
+            SJBG_BARRIER();
             uint32_t run = carry_s + warp_tot[warp_id()] + ex;
 #pragma unroll
             for (uint32_t k = 0; k < kItems; k++) {
@@ -265,9 +265,9 @@ __global__ void __launch_bounds__(1024) part_scan_kernel(const uint32_t *__restr
                 }
                 run += v[k];
             }
-            __syncthreads();
+            SJBG_BARRIER();
             if (threadIdx.x == blockDim.x - 1) carry_s = run;
-            __syncthreads();
+            SJBG_BARRIER();
         }
     }
 }
@@ -281,19 +281,19 @@ __device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
     uint32_t tot;
     uint32_t ex = warp_excl_scan(s, &tot);
     if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
-    __syncthreads();
+    SJBG_BARRIER();
     if (warp_id() == 0) {
         uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0, tt;
         warp_tot[lane_id()] = warp_excl_scan(x, &tt);
     }
-    __syncthreads();
+    SJBG_BARRIER();
     uint32_t run = warp_tot[warp_id()] + ex;
     for (uint32_t i = b0; i < b1; i++) {
         uint32_t c = a[i];
         a[i] = run;
         run += c;
     }
-    __syncthreads();
+    SJBG_BARRIER();
 }
 
 // ------------------------------------------------------------------ 3. scatter
@@ -328,7 +328,7 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) lcnt[i] = 0;
     if (threadIdx.x == 0) kept_s = 0;
     if (heavy) heavy_set_load(hs, cls.m);
-    __syncthreads();
+    SJBG_BARRIER();
     constexpr int kPer = kTile / kPartThreads;
     uint64_t e[kPer];
     uint32_t bk[kPer], rk[kPer];
@@ -352,7 +352,7 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
             }
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     // reserve one global range per non-empty bucket
     uint32_t *gcur = cursor + (right ? B : 0) + wp.bucket_base;
     uint32_t kept = 0;
@@ -372,7 +372,7 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
             sb[pos] = (uint16_t)bk[k];
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     uint64_t *out = right ? outR : outL;
     for (uint32_t j = threadIdx.x; j < nk; j += blockDim.x) {
         const uint32_t b = sb[j];
@@ -485,7 +485,7 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
             t.sumf[i] = 0;
         }
         if (threadIdx.x == 0) novf = 0;
-        __syncthreads();
+        SJBG_BARRIER();
         // build: kJoinPer independent loads per thread, then insert them
         for (uint32_t base = 0; base < n; base += tile) {
             uint64_t e[kJoinPer];
@@ -494,7 +494,7 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
                 const uint32_t i = base + k * blockDim.x + threadIdx.x;
                 e[k] = i < n ? Rb[i] : 0ull;
             }
-            __syncthreads();   // every read of this tile precedes any overflow write
+            SJBG_BARRIER();   // every read of this tile precedes any overflow write
 #pragma unroll
             for (int k = 0; k < kJoinPer; k++) {
                 const uint32_t i = base + k * blockDim.x + threadIdx.x;
@@ -503,7 +503,7 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
                 if (valid && !ok) Rb[atomicAdd(&novf, 1u)] = e[k];
             }
         }
-        __syncthreads();
+        SJBG_BARRIER();
         // probe: the same independent-load tiling, no barriers needed
         for (uint32_t base = 0; base < nS; base += tile) {
             uint64_t e[kJoinPer];
@@ -524,9 +524,9 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
                 }
             }
         }
-        __syncthreads();
+        SJBG_BARRIER();
         n = novf;
-        __syncthreads();
+        SJBG_BARRIER();
         if (n == 0) break;
     }
     flush_acc(&acc[bucket_win[b]], count, 0, prod);
@@ -562,26 +562,32 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
             keys[i] = kEmptyKey;
             head[i] = kNil;
         }
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-            const uint64_t e = Rb[c0 + i];
-            const uint32_t key = (uint32_t)e;
-            vals[i] = (uint32_t)(e >> 32);
-            uint32_t s;
-            if (key == kEmptyKey) {
-                s = C;
-            } else {
-                s = slot_hash(key, table_bits);
-                // at most m <= C/2 keys: a free or matching slot exists within C probes
-                for (uint32_t p = 0; p < C; p++) {
-                    const uint32_t prev = atomicCAS(&keys[s], kEmptyKey, key);
-                    if (prev == kEmptyKey || prev == key) break;
-                    s = (s + 1) & (C - 1);
+        SJBG_BARRIER();
+        // insert: the trip count is uniform per block (bounds checked inside), and
+        // every warp reconverges before the barrier
+        for (uint32_t i0 = 0; i0 < m; i0 += blockDim.x) {
+            const uint32_t i = i0 + threadIdx.x;
+            if (i < m) {
+                const uint64_t e = Rb[c0 + i];
+                const uint32_t key = (uint32_t)e;
+                vals[i] = (uint32_t)(e >> 32);
+                uint32_t s;
+                if (key == kEmptyKey) {
+                    s = C;
+                } else {
+                    s = slot_hash(key, table_bits);
+                    // at most m <= C/2 keys: a free or matching slot exists within C probes
+                    for (uint32_t p = 0; p < C; p++) {
+                        const uint32_t prev = atomicCAS(&keys[s], kEmptyKey, key);
+                        if (prev == kEmptyKey || prev == key) break;
+                        s = (s + 1) & (C - 1);
+                    }
                 }
+                next[i] = atomicExch(&head[s], i);
             }
-            next[i] = atomicExch(&head[s], i);
+            __syncwarp();
         }
-        __syncthreads();
+        SJBG_BARRIER();
         // probe: loop bound is uniform per warp so the pair reservation can use shuffles
         for (uint32_t j0 = 0; j0 < nS; j0 += blockDim.x) {
             const uint32_t j = j0 + threadIdx.x;
@@ -606,7 +612,8 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
             }
             uint32_t mine = 0;
             const unsigned long long gs = sjbg_gs(sv);
-            for (uint32_t i = h; i != kNil; i = next[i]) {
+            // chains link indices of this chunk: a walk never takes more than m steps
+            for (uint32_t i = h, steps = 0; i < m && steps < m; i = next[i], steps++) {
                 const uint32_t rv = vals[i];
                 xr ^= sjbg_pair_hash(rv, sv);
                 prod += sjbg_fr(rv) * gs;
@@ -619,13 +626,14 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
                 unsigned long long base = 0;
                 if (lane_id() == 0 && tot) base = atomicAdd(&acc[w].npairs, (unsigned long long)tot);
                 base = __shfl_sync(0xFFFFFFFFu, base, 0) + ex;
-                for (uint32_t i = h; i != kNil; i = next[i]) {
+                for (uint32_t i = h, steps = 0; i < m && steps < m; i = next[i], steps++) {
                     if (base < pcap) pout[base] = sjbg_pair{vals[i], sv};
                     base++;
                 }
             }
+            __syncwarp();
         }
-        __syncthreads();
+        SJBG_BARRIER();
     }
     flush_acc(&acc[w], count, xr, prod);
 }
@@ -643,9 +651,9 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
     }
     __shared__ uint32_t item_s;
     for (;;) {
-        __syncthreads();
+        SJBG_BARRIER();
         if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
-        __syncthreads();
+        SJBG_BARRIER();
         const uint32_t b = item_s;
         if (b >= B) break;
         join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, table_bits);
@@ -664,9 +672,9 @@ bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__re
     }
     __shared__ uint32_t item_s;
     for (;;) {
-        __syncthreads();
+        SJBG_BARRIER();
         if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
-        __syncthreads();
+        SJBG_BARRIER();
         const uint32_t b = item_s;
         if (b >= B) break;
         join_enum_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs, table_bits);
@@ -779,11 +787,12 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     // persistent CTAs draining a work queue of buckets, or one CTA per bucket
     uint32_t *queue = nullptr;
     dim3 jgrid((uint32_t)B);
-    if (h->tune.persistent_join && B > (uint64_t)h->num_sms) {
+    // (chain-building joins keep one CTA per bucket)
+    if (!enumerate && h->tune.persistent_join && B > (uint64_t)h->num_sms) {
         queue = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_WIN, 64));
         if (!queue) return fail(h, SJBG_E_NOMEM, "work queue");
         SJBG_CK(h, cudaMemsetAsync(queue, 0, 4, h->stream));
-        jgrid = dim3((uint32_t)std::min<uint64_t>(B, (uint64_t)h->num_sms * (enumerate ? 1 : 1)));
+        jgrid = dim3((uint32_t)std::min<uint64_t>(B, (uint64_t)h->num_sms));
     }
     if (enumerate) {
         const uint32_t bits = 13;   // 8192 slots for chunks of 4096

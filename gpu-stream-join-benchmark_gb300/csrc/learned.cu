@@ -158,7 +158,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     // ---- heavy keys: bitonic sort of the candidates (descending), keep the top
     const uint32_t nc = min(scr[w].n_cand, kCandMax);
     for (uint32_t i = threadIdx.x; i < kCandMax; i += blockDim.x) sc[i] = i < nc ? cand[(uint64_t)w * kCandMax + i] : 0ull;
-    __syncthreads();
+    SJBG_BARRIER();
     for (uint32_t k = 2; k <= kCandMax; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
             for (uint32_t i = threadIdx.x; i < kCandMax; i += blockDim.x) {
@@ -169,7 +169,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
                     if (desc ? (a < b) : (a > b)) { sc[i] = b; sc[p] = a; }
                 }
             }
-            __syncthreads();
+            SJBG_BARRIER();
         }
     }
     if (threadIdx.x == 0) {
@@ -187,7 +187,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         }
         n_heavy_s = h;
     }
-    __syncthreads();
+    SJBG_BARRIER();
     const uint32_t nh = n_heavy_s;
     for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) {
         const uint32_t key = ~(uint32_t)sc[h];
@@ -195,7 +195,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         M.heavy_keys[h] = key;
         atomicSub(&hw[bin_of(key_x(key, kmin, inv))], c);   // light histogram only
     }
-    __syncthreads();
+    SJBG_BARRIER();
     heavy_set_build(M.heavy_set, M.heavy_keys, nh);
 
     // ---- light CDF at bin upper edges: in-place exclusive scan, then cdf_j = incl_j / total
@@ -206,14 +206,14 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     uint32_t tot;
     const uint32_t ex = warp_excl_scan(loc, &tot);
     if (lane_id() == 31) warp_tot[warp_id()] = ex + loc;
-    __syncthreads();
+    SJBG_BARRIER();
     if (warp_id() == 0) {
         uint32_t x = warp_tot[lane_id()], tt;
         const uint32_t e = warp_excl_scan(x, &tt);
         warp_tot[lane_id()] = e;
         if (lane_id() == 31) light_total_s = e + x;
     }
-    __syncthreads();
+    SJBG_BARRIER();
     const uint32_t total = light_total_s;
     uint32_t run = warp_tot[warp_id()] + ex;
     for (uint32_t i = 0; i < per; i++) {
@@ -226,7 +226,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         lmax[threadIdx.x] = -1.0f;
     }
     if (threadIdx.x < 4) rootsum[threadIdx.x] = 0.0;
-    __syncthreads();
+    SJBG_BARRIER();
     const float invt = total ? 1.0f / (float)total : 0.0f;
 
     // ---- root line y = a x + b over all bin points (x_j = (j+1)/kBins, y_j = cdf_j)
@@ -248,7 +248,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         atomicAdd(&rootsum[2], sxx);
         atomicAdd(&rootsum[3], sxy);
     }
-    __syncthreads();
+    SJBG_BARRIER();
     const double nn = kBins;
     const double den = nn * rootsum[2] - rootsum[0] * rootsum[0];
     double ra = den != 0.0 ? (nn * rootsum[3] - rootsum[0] * rootsum[1]) / den : 1.0;
@@ -295,7 +295,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             }
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     {
         int cur = -1;
         float sxy = 0.f, sxx = 0.f, mx = 0.f, my = 0.f;
@@ -327,7 +327,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             }
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     if (threadIdx.x == 0) {
         // monotone clamps: empty leaves inherit the previous upper bound
         float prev = 0.0f;
@@ -379,14 +379,14 @@ learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint3
     LearnedModel &M = models[w];
     if (M.fallback) return;
     if (threadIdx.x == 0) { mx_s = 0; sum_s = 0; }
-    __syncthreads();
+    SJBG_BARRIER();
     const uint32_t P = 1u << wins[w].log2_buckets;
     const uint32_t *pw = pred + (uint64_t)w * kPredStride;
     uint32_t mx = 0, sm = 0;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) { mx = max(mx, pw[i]); sm += pw[i]; }
     atomicMax(&mx_s, mx);
     atomicAdd(&sum_s, sm);
-    __syncthreads();
+    SJBG_BARRIER();
     if (threadIdx.x == 0) {
         const float mean = (float)sum_s / (float)P;
         // a window whose light sample is too small to judge keeps its model

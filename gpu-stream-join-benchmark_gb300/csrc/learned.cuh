@@ -63,7 +63,7 @@ __device__ __forceinline__ void heavy_set_build(HeavySet &hs, const uint32_t *ke
         hs.keys[i] = kEmptyKey;
         hs.idx[i] = 0xFFFFFFFFu;
     }
-    __syncthreads();
+    SJBG_BARRIER();
     for (uint32_t h = threadIdx.x; h < n; h += blockDim.x) {
         const uint32_t key = keys[h];
         uint32_t s = heavy_slot(key);
@@ -76,7 +76,7 @@ __device__ __forceinline__ void heavy_set_build(HeavySet &hs, const uint32_t *ke
             s = (s + 1) & (kHeavySlots - 1);
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
 }
 
 // Copy a model's prebuilt heavy-key set into shared memory (all threads; ends with a barrier).
@@ -84,7 +84,7 @@ __device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel 
     const uint4 *src = reinterpret_cast<const uint4 *>(&m->heavy_set);
     uint4 *dst = reinterpret_cast<uint4 *>(&hs);
     for (uint32_t i = threadIdx.x; i < sizeof(HeavySet) / 16; i += blockDim.x) dst[i] = src[i];
-    __syncthreads();
+    SJBG_BARRIER();
 }
 
 // Index of `key` among the heavy keys, or kHeavyBucket when it is light.

@@ -68,7 +68,7 @@ __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uin
     for (uint32_t c0 = r0; c0 < r_end; c0 += kChunk) {
         const uint32_t m = min(kChunk, r_end - c0);
         const uint32_t mpad = (m + kVote - 1) / kVote * kVote;
-        __syncthreads();
+        SJBG_BARRIER();
         for (uint32_t i = threadIdx.x; i < mpad; i += kNljThreads) {
             if (i < m) {
                 const uint2 t = __ldg(reinterpret_cast<const uint2 *>(Rw + c0 + i));
@@ -79,7 +79,7 @@ __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uin
                 rvals[i] = 0;
             }
         }
-        __syncthreads();
+        SJBG_BARRIER();
         const uint4 *rk4 = reinterpret_cast<const uint4 *>(rkeys);
         for (uint32_t r = 0; r < mpad; r += kVote) {
             bool p = false;

@@ -100,7 +100,7 @@ merge_join_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict_
     const unsigned long long *Fa = F + mw.a_off;
     const uint32_t m = i1 - i0;
     for (uint32_t i = threadIdx.x; i < m; i += kMergeThreads) sa[i] = A[i0 + i];
-    __syncthreads();
+    SJBG_BARRIER();
     const uint64_t pcap = kPairs ? mw.pairs_cap : 0;
     sjbg_pair *pout = kPairs ? pairs + mw.pairs_off : nullptr;
 

@@ -125,7 +125,7 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
     const uint32_t tl = blockIdx.x - sg.tile0;
     const uint32_t base = tl * kSortTile;
     hist[threadIdx.x] = 0;
-    __syncthreads();
+    SJBG_BARRIER();
     const uint4 *k4 = reinterpret_cast<const uint4 *>(keys + sg.off + base);
     constexpr int kPer = kSortTile / 4 / 256;   // 4 vectors per thread
     uint4 v[kPer];
@@ -144,7 +144,7 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
             if (valid && lane_id() == (uint32_t)(__ffs(grp) - 1)) atomicAdd(&hist[d], (uint32_t)__popc(grp));
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl] = hist[threadIdx.x];
 }
 
@@ -157,7 +157,7 @@ rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs) 
     uint32_t *c = counts + (uint64_t)sg.tile0 * kDigits;
     const uint32_t n = kDigits * sg.ntiles;
     if (threadIdx.x == 0) carry_s = 0;
-    __syncthreads();
+    SJBG_BARRIER();
     constexpr uint32_t kItems = 4;
     for (uint32_t base = 0; base < n; base += blockDim.x * kItems) {
         uint32_t v[kItems], s = 0;
@@ -170,13 +170,13 @@ rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs) 
         uint32_t wt;
         const uint32_t ex = warp_excl_scan(s, &wt);
         if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
-        __syncthreads();
+        SJBG_BARRIER();
         if (warp_id() == 0) {
             const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0;
             uint32_t tt;
             warp_tot[lane_id()] = warp_excl_scan(x, &tt);
         }
-        __syncthreads();
+        SJBG_BARRIER();
         uint32_t run = carry_s + warp_tot[warp_id()] + ex;
 #pragma unroll
         for (uint32_t k = 0; k < kItems; k++) {
@@ -184,9 +184,9 @@ rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs) 
             if (i < n) c[i] = run;
             run += v[k];
         }
-        __syncthreads();
+        SJBG_BARRIER();
         if (threadIdx.x == blockDim.x - 1) carry_s = run;
-        __syncthreads();
+        SJBG_BARRIER();
     }
 }
 
@@ -218,7 +218,7 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
 
     if (threadIdx.x == 0) mbar_init(&sm.bar, 1);
     for (uint32_t i = threadIdx.x; i < kSortWarps * (kDigits + 1); i += kSortThreads) (&sm.wcnt[0][0])[i] = 0;
-    __syncthreads();
+    SJBG_BARRIER();
     if (threadIdx.x == 0) {
         mbar_expect_tx(&sm.bar, 2 * kSortTile * 4);
         bulk_g2s(sm.in_keys, keys + sg.off + base, kSortTile * 4, &sm.bar);
@@ -250,7 +250,7 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
         if (lane == (uint32_t)(__ffs(peers) - 1)) sm.wcnt[w][d] = cur + __popc(peers);
         __syncwarp();
     }
-    __syncthreads();
+    SJBG_BARRIER();
     // per digit: exclusive scan over warps, tile total in `loc`
     if (threadIdx.x < kDigits) {
         uint32_t run = 0;
@@ -261,7 +261,7 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
         }
         sm.loc[threadIdx.x] = run;
     }
-    __syncthreads();
+    SJBG_BARRIER();
     // exclusive scan of the 256 digit totals (8 warps x 32 digits)
     if (threadIdx.x < kDigits) {
         const uint32_t x = sm.loc[threadIdx.x];
@@ -271,13 +271,13 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
         __syncwarp();
         sm.loc[threadIdx.x] = ex;   // partial; warp offsets added below
     }
-    __syncthreads();
+    SJBG_BARRIER();
     if (threadIdx.x < kDigits) {
         uint32_t add = 0;
         for (uint32_t ww = 0; ww < w; ww++) add += sm.warp_tot[ww];
         sm.loc[threadIdx.x] += add;
     }
-    __syncthreads();
+    SJBG_BARRIER();
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
         const uint32_t pos = w * (kSortTile / kSortWarps) + k * 32 + lane;
@@ -288,7 +288,7 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
             sm.out_vals[p] = sm.in_vals[pos];
         }
     }
-    __syncthreads();
+    SJBG_BARRIER();
     for (uint32_t j = threadIdx.x; j < n; j += kSortThreads) {
         const uint32_t k = sm.out_keys[j];
         const uint32_t d = (k >> shift) & 0xFFu;
@@ -312,7 +312,7 @@ fr_tile_sum_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict_
         if (base + i < sg.n) acc += sjbg_fr(vals[sg.off + base + i]);
     acc = warp_sum_u64(acc);
     if (lane_id() == 0) ws[warp_id()] = acc;
-    __syncthreads();
+    SJBG_BARRIER();
     if (threadIdx.x == 0) {
         unsigned long long t = 0;
         for (int i = 0; i < 8; i++) t += ws[i];
@@ -351,7 +351,7 @@ fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict
         if (lane_id() >= (uint32_t)o) x += y;
     }
     if (lane_id() == 31) wsum[warp_id()] = x;
-    __syncthreads();
+    SJBG_BARRIER();
     unsigned long long wofs = 0;
     for (uint32_t ww = 0; ww < warp_id(); ww++) wofs += wsum[ww];
     unsigned long long run = tsum[blockIdx.x] + wofs + x - loc;

@@ -71,6 +71,7 @@ static uint32_t log2u(uint64_t x) {
 int autotune_lazy(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                   bool enumerate) {
     if (h->cfg.algorithm != SJBG_ALG_HJ || n == 0) return SJBG_OK;   // only the hash join has tunables
+    if (std::getenv("SJBG_BUCKET_TARGET") || std::getenv("SJBG_PERSISTENT_JOIN")) return SJBG_OK;   // pinned by the user
     tune_load(h);
     uint64_t total = 0;
     for (uint32_t w = 0; w < n; w++) total += wins[w].n_left + wins[w].n_right;
@@ -89,6 +90,7 @@ int autotune_lazy(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     best.ms = 1e30f;
     for (uint32_t target : {2048u, 4096u, 8192u}) {
         for (bool persistent : {false, true}) {
+            if (enumerate && persistent) continue;   // chain-building joins run one CTA per bucket
             h->tune.bucket_target = target;
             h->tune.persistent_join = persistent;
             uint32_t pu;
