@@ -149,13 +149,241 @@ def algorithmic_bytes(kernel, nwin, W, light_frac):
     return None
 
 
+# ---------------------------------------------------------------------------- other workloads
+def _line(metric, value, unit, ms, args, workload, extra, higher=True):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+           "data": "synthetic", "config": {"workload": workload}}
+    out.update(extra)
+    return out
+
+
+def _events_time(torch, stream, fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def bench_batched(args, sjbg, torch, dev):
+    """1,024 windows, sizes log-uniform in [2^10, 2^20] (seed 4), keys in [0, 4W):
+    hash join (autotuned, graph-replayed) and sort-merge join in one call each."""
+    import ctypes as C
+    sizes = [sjbg_log_uniform(w) for w in range(1024)]
+    total = sum(sizes)
+    dl = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    dr = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    descs_l, off = [], 0
+    hj = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, flags=sjbg.F_GRAPH | sjbg.F_AUTOTUNE, max_tuples_per_window=1 << 20,
+                     device=dev)
+    smj = sjbg.Joiner(sjbg.ALG_SMJ, sjbg.LAZY, flags=sjbg.F_GRAPH, max_tuples_per_window=1 << 20, device=dev)
+    for n in sizes:
+        hj.generate(dl.data_ptr() + 16 * off, off, n, 1, 4 * n)
+        hj.generate(dr.data_ptr() + 16 * off, off, n, 2, 4 * n)
+        descs_l.append((off, n, off, n, 0, 0))
+        off += n
+    descs = (sjbg.WindowDesc * 1024)(*[sjbg.WindowDesc(*d) for d in descs_l])
+    res_h, res_s = (sjbg.WindowResult * 1024)(), (sjbg.WindowResult * 1024)()
+    for j in (hj, smj):
+        j.set_stream(stream.cuda_stream)
+    ms_h = _events_time(torch, stream, lambda: hj.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res_h),
+                        args.steps, args.warmup)
+    ms_s = _events_time(torch, stream, lambda: smj.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res_s),
+                        max(1, args.steps // 2), 2)
+    same = [(a.count, a.prod_checksum) for a in res_h] == [(a.count, a.prod_checksum) for a in res_s]
+    hj.close()
+    smj.close()
+    tuples = 2 * total
+    return _line("joined input tuples/s", tuples / (ms_h * 1e-3), "tuples/s", ms_h, args, "batched_1024",
+                 {"sort_merge": {"value": tuples / (ms_s * 1e-3), "ms_per_step": ms_s},
+                  "outputs_identical_hash_vs_sort_merge": same, "tuples_per_step": tuples,
+                  "notes": "hash join autotuned + CUDA-graph replay; sort-merge graph replay (4 radix passes)"})
+
+
+def sjbg_log_uniform(w, lo=1 << 10, hi=1 << 20, seed=4):
+    """Window length w of the batched workload (the generator's log-uniform draw)."""
+    import math
+    x = seed
+    # SplitMix64 draw w of stream `seed`, as in csrc/sjbg_gen.h
+    M = (1 << 64) - 1
+
+    def mix(z):
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        return z ^ (z >> 31)
+    g = 0x9E3779B97F4A7C15
+    st = mix((x + g) & M)
+    r = mix((st + (w + 1) * g) & M)
+    u = (r >> 11) * (1.0 / 9007199254740992.0)
+    v = 2.0 ** (math.log2(lo) + u * (math.log2(hi) - math.log2(lo)))
+    return max(lo, min(hi, int(v)))
+
+
+def bench_eager(args, sjbg, torch, dev, algo, W, D, n_batches):
+    """Eager joins over batches of 4,096 (L0,R0,L1,R1,...; the reference's close rule)."""
+    B = 4096
+    n = n_batches * B
+    dl = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    dr = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    a = sjbg.ALG_SMJ if algo == "SMJ" else (sjbg.ALG_NLJ if algo == "NLJ" else sjbg.ALG_HJ)
+    j = sjbg.Joiner(a, sjbg.EAGER, batch_size=B, window_size=W, max_tuples_per_window=W, device=dev)
+    j.generate(dl.data_ptr(), 0, n, 1, D)
+    j.generate(dr.data_ptr(), 0, n, 2, D)
+    stream = torch.cuda.Stream()
+    j.set_stream(stream.cuda_stream)
+    out = {}
+
+    def step():
+        out["r"] = j.eager_run(dl, dr, n_batches, mem=sjbg.MEM_DEVICE)
+    ms = _events_time(torch, stream, step, max(1, args.steps // 2), 1)
+    bc, wins = out["r"]
+    j.close()
+    tuples = 2 * n
+    return _line("joined input tuples/s", tuples / (ms * 1e-3), "tuples/s", ms, args, f"eager_{algo.lower()}",
+                 {"window": W, "batch": B, "batches_per_side": n_batches, "key_domain": D,
+                  "windows": sum(1 for w in wins if w["status"] == 0),
+                  "matches": int(bc.sum()), "per_batch_latency_ms": ms / (2 * n_batches)})
+
+
+def bench_eager_smj(args, sjbg, torch, dev):
+    return bench_eager(args, sjbg, torch, dev, "SMJ", 1 << 20, 1 << 20, 1024)
+
+
+def bench_eager_nlj(args, sjbg, torch, dev):
+    return bench_eager(args, sjbg, torch, dev, "NLJ", 65536, 65536, 64)
+
+
+def bench_stream(args, sjbg, torch, dev, rate=1e9, seconds=3.0, window_ms=100, chunk_ms=5.0):
+    """Streaming loop paced in real time: Poisson batches of 4,096 per stream at
+    `rate` tuples/s (both streams together), 100 ms event-time windows, Zipf keys
+    over [0, 2^26) whose exponent steps 0.8 -> 1.2 -> 1.5 (every seconds/3 here),
+    learned partitioning refitted per window, 120 GB HBM budget."""
+    import numpy as np
+    D, B = 1 << 26, 4096
+    tables = {z: torch.from_numpy(sjbg.zipf_table(D, z).view(np.int64)).cuda() for z in (0.8, 1.2, 1.5)}
+    j = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, partitioner=sjbg.PART_LEARNED, max_tuples_per_window=1 << 30,
+                    hbm_budget_bytes=120 << 30, device=dev)
+    rng = np.random.default_rng(7)
+    per_side = rate / 2.0
+    gap_ns = B / per_side * 1e9
+    chunk_ns = int(chunk_ms * 1e6)
+    cap = int(per_side * chunk_ms * 1e-3 * 2) + 2 * B
+    bufs = [torch.empty(cap * 16, dtype=torch.uint8, device="cuda") for _ in range(2)]
+    next_t = [rng.exponential(gap_ns), rng.exponential(gap_ns)]
+    first = [0, 0]
+    j.stream_open(window_ms * 1_000_000)
+    t0 = time.perf_counter()
+    end_ns = int(seconds * 1e9)
+    pushed = 0
+    results = []
+    t_ev = 0
+    while t_ev < end_ns:
+        t_ev += chunk_ns
+        for side in (0, 1):
+            times = []
+            while next_t[side] < t_ev:
+                times.append(int(next_t[side]))
+                next_t[side] += rng.exponential(gap_ns)
+            if not times:
+                continue
+            n = len(times) * B
+            z = 0.8 if times[0] < end_ns / 3 else (1.2 if times[0] < 2 * end_ns / 3 else 1.5)
+            buf = bufs[side]
+            j.generate(buf.data_ptr(), first[side], n, 1 + side, D, tables[z].data_ptr(), 3)
+            ts = torch.tensor(times, dtype=torch.int64, device="cuda").repeat_interleave(B)
+            buf[:n * 16].view(torch.int64).view(-1, 2)[:, 1] = ts
+            first[side] += n
+            # pace: do not push data before its event time has come (wall clock)
+            wait = times[-1] * 1e-9 - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            j.stream_push(buf, side == 0, mem=sjbg.MEM_DEVICE, n=n)
+            pushed += n
+        results += j.stream_poll(4096)
+    st = j.stream_close()
+    wall = time.perf_counter() - t0
+    results += j.stream_poll(4096)
+    j.close()
+    sustained = st["p99_ms"] < window_ms
+    return _line("joined input tuples/s", st["tuples_joined"] / wall, "tuples/s", wall * 1e3, args,
+                 f"stream_{rate / 1e9:g}g",
+                 {"offered_rate_tuples_per_s": rate, "event_seconds": seconds, "window_ms": window_ms,
+                  "latency": {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "unit": "ms close-to-result"},
+                  "windows": st["windows_closed"], "rejected": st["windows_rejected"], "fallbacks": st["fallbacks"],
+                  "tuples_pushed": pushed, "join_busy_ms": st["busy_ms"], "keeps_up": sustained,
+                  "notes": "real-time paced; Zipf exponent drift compressed to thirds of the run"})
+
+
+SPECIAL = {
+    "batched_1024": bench_batched,
+    "eager_smj_2p20": bench_eager_smj,
+    "eager_nlj_65536": bench_eager_nlj,
+    "stream_0.5g": lambda a, s, t, d: bench_stream(a, s, t, d, rate=0.5e9),
+    "stream_1g": lambda a, s, t, d: bench_stream(a, s, t, d, rate=1e9),
+    "stream_2g": lambda a, s, t, d: bench_stream(a, s, t, d, rate=2e9),
+    "stream_4g": lambda a, s, t, d: bench_stream(a, s, t, d, rate=4e9),
+}
+
+
+def run_reference_special(args, workload):
+    """CPU arm for the other workloads: the restated reference joiners on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as O
+    cores = os.cpu_count() or 1
+    t_total, tuples = 0.0, 0
+    if workload == "batched_1024":
+        for w in range(0, 1024, 64):   # a sample of 16 windows, lazy CPU_HJ with all cores probing
+            n = sjbg_log_uniform(w)
+            l = O.gen_uniform(0, n, 1, 4 * n, cores)
+            r = O.gen_uniform(0, n, 2, 4 * n, cores)
+            t = time.perf_counter()
+            O.lazy_hj_count(l, r, 4 * n, n, cores)
+            t_total += time.perf_counter() - t
+            tuples += 2 * n
+        sample = "16 of the 1,024 windows, lazy CPU_HJ restated"
+    elif workload.startswith("eager"):
+        W, D, nb = (1 << 20, 1 << 20, 128) if "smj" in workload else (65536, 65536, 32)
+        l = O.gen_uniform(0, nb * 4096, 1, D, cores)
+        r = O.gen_uniform(0, nb * 4096, 2, D, cores)
+        t = time.perf_counter()
+        O.eager_hj(l, r, 4096, W, D)
+        t_total = time.perf_counter() - t
+        tuples = 2 * nb * 4096
+        sample = f"{nb} batches per side, eager CPU_HJ restated (bucket chains)"
+    else:
+        n = 1 << 24
+        T = O.zipf_table(1 << 26, 1.2)
+        l = O.gen_zipf(0, n, 1, T, 1 << 26, 3, cores)
+        r = O.gen_zipf(0, n, 2, T, 1 << 26, 3, cores)
+        t = time.perf_counter()
+        O.lazy_smj_count(l, r, 1 << 26, cores)
+        t_total = time.perf_counter() - t
+        tuples = 2 * n
+        sample = "one recorded window of 2^24 tuples per stream, lazy CPU_SMJ restated"
+    value = tuples / t_total
+    return {"metric": "joined input tuples/s", "value": value, "unit": "tuples/s", "n_gpus": args.gpus,
+            "steps": 1, "warmup": 0, "ms_per_step": t_total * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="skewed_hj_z1.5", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="skewed_hj_z1.5", choices=sorted(WORKLOADS) + sorted(SPECIAL))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
 
@@ -163,7 +391,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args, args.workload)))
+            ref = run_reference_special if args.workload in SPECIAL else run_reference
+            print(json.dumps(ref(args, args.workload)))
         return
 
     import numpy as np
@@ -177,18 +406,20 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
+    if args.workload in SPECIAL:
+        out = SPECIAL[args.workload](args, sjbg, torch, local)
+        if rank == 0:
+            print(json.dumps(out))
+        return
     nwin, W, D, z = WORKLOADS[args.workload]
     total = nwin * W
 
     # ---- inputs generated in HBM (same draws as the host generator)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     dL = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
     dR = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
     table_ptr = None
     if z is not None:
-        import oracle_py as O  # host Zipf CDF table (generator input, not the checker)
-
-        T = O.zipf_table(D, z)
+        T = sjbg.zipf_table(D, z)   # generator input (host CDF table), uploaded once
         dT = torch.from_numpy(T.view(np.int64)).cuda()
         table_ptr = dT.data_ptr()
     flags_common = dict(algorithm=sjbg.ALG_HJ, progressiveness=sjbg.LAZY, max_tuples_per_window=W, device=local)

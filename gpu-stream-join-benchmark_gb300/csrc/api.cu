@@ -469,6 +469,12 @@ int sjbg_generate(sjbg_handle *h, sjbg_tuple *dev_out, uint64_t first, uint64_t 
     return SJBG_OK;
 }
 
+int sjbg_zipf_table(uint64_t *table, uint64_t n, double z) {
+    if (!table || n == 0 || !(z >= 0.0)) return SJBG_E_INVALID;
+    sjbg_zipf_table_fill(table, n, z);
+    return SJBG_OK;
+}
+
 int sjbg_kernel_stats(sjbg_handle *h, uint32_t index, char *name, size_t name_len, uint64_t *launches,
                       double *total_ms) {
     if (!h) return SJBG_E_INVALID;

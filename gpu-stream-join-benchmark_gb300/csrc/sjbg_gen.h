@@ -120,7 +120,7 @@ SJBG_HD uint32_t sjbg_zipf_rank(const uint64_t *table, uint64_t n, uint64_t u) {
     return (uint32_t)lo;
 }
 
-#if !defined(__CUDA_ARCH__)
+/* (the two functions below are plain static inline, i.e. host-only under nvcc) */
 /* Host-only: fill the Zipf CDF table (n entries, exponent z >= 0).  Weights
  * are summed in IEEE double with Kahan compensation (no products inside the
  * sums, so FMA contraction cannot change the result between compilers). */
@@ -156,6 +156,4 @@ static inline uint64_t sjbg_log_uniform(uint64_t seed, uint64_t w, uint64_t lo, 
     if (r > hi) r = hi;
     return r;
 }
-#endif
-
 #endif /* SJBG_GEN_H */

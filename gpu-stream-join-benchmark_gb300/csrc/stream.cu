@@ -91,7 +91,7 @@ static void release_buffers(sjbg_handle *h, StreamState &st, StreamWin *w) {
 static void harvest(sjbg_handle *h, StreamState &st, bool wait) {
     while (!st.wins.empty()) {
         StreamWin *w = st.wins.front();
-        if (w->state == 0) break;   // still open
+        if (w->state == 0 || w->state == 2) break;   // still open
         sjbg_window_result r;
         std::memset(&r, 0, sizeof(r));
         if (w->state == 1) {
@@ -131,7 +131,10 @@ static int launch_join(sjbg_handle *h, StreamState &st, StreamWin *w, cudaStream
     st.closed++;
     st.any_closed = true;
     st.last_closed_id = w->id;
-    if (w->state == 2) return SJBG_OK;   // rejected: nothing to join
+    if (w->state == 2) {   // rejected: nothing to join, its result reports the refusal
+        w->state = 3;
+        return SJBG_OK;
+    }
     // close marker on an idle stream: the window's latency includes queueing
     SJBG_CK(h, cudaEventRecord(w->ev_close, side));
     SJBG_CK(h, cudaStreamWaitEvent(h->stream, w->ev_close, 0));
@@ -151,7 +154,7 @@ static int launch_join(sjbg_handle *h, StreamState &st, StreamWin *w, cudaStream
 static int close_ready(sjbg_handle *h, StreamState &st, cudaStream_t side, bool all) {
     const uint64_t wm = std::min(st.seen[0] ? st.wm[0] : 0, st.seen[1] ? st.wm[1] : 0);
     for (StreamWin *w : st.wins) {
-        if (w->state != 0) continue;
+        if (w->state != 0 && w->state != 2) continue;
         const uint64_t end = (w->id + 1) * st.window_ns;
         if (!all && !(st.seen[0] && st.seen[1] && end <= wm)) break;
         int rc = launch_join(h, st, w, side);

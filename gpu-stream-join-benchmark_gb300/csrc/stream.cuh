@@ -14,7 +14,7 @@ struct StreamWin {
     uint64_t id = 0;
     sjbg_tuple *buf[2] = {nullptr, nullptr};
     uint64_t n[2] = {0, 0}, cap[2] = {0, 0};
-    int state = 0;               // 0 open, 1 join enqueued, 2 rejected
+    int state = 0;               // 0 open, 1 join enqueued, 2 rejected (still open), 3 rejected and closed
     cudaEvent_t ev_close = nullptr, ev_done = nullptr;
     DevBuf pinned[6];            // private staging of this window's join
     uint32_t part_used = 0;

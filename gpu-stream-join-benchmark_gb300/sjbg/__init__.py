@@ -40,7 +40,7 @@ EXPORTS = [
     "sjbg_eager_execute", "sjbg_eager_clear_states", "sjbg_eager_window_result", "sjbg_eager_end_of_stream",
     "sjbg_eager_run", "sjbg_stream_open", "sjbg_stream_push", "sjbg_stream_poll", "sjbg_stream_close",
     "sjbg_generate", "sjbg_kernel_stats", "sjbg_kernel_stats_reset", "sjbg_launch_count",
-    "sjbg_lazy_hj_noalloc",
+    "sjbg_lazy_hj_noalloc", "sjbg_zipf_table",
 ]
 
 
@@ -116,6 +116,7 @@ def load(path: str = LIB_PATH):
         L.sjbg_launch_count.argtypes = [vp]
         L.sjbg_launch_count.restype = u64
         L.sjbg_lazy_hj_noalloc.argtypes = [vp, u64, vp, u64, vp, vp]
+        L.sjbg_zipf_table.argtypes = [vp, u64, C.c_double]
         _lib = L
     return _lib
 
@@ -138,6 +139,15 @@ def _len(a, dtype=TUPLE_DTYPE) -> int:
     if hasattr(a, "numel") and hasattr(a, "element_size"):
         return a.numel() * a.element_size() // dtype.itemsize
     raise TypeError("length of a device buffer must be given explicitly")
+
+
+def zipf_table(n: int, z: float) -> np.ndarray:
+    """Zipf(z) CDF table over n ranks for sjbg_generate (host memory)."""
+    t = np.empty(n, np.uint64)
+    rc = load().sjbg_zipf_table(t.ctypes.data_as(C.c_void_p), n, z)
+    if rc:
+        raise SjbgError(rc, "bad Zipf table arguments")
+    return t
 
 
 def lazy_hj_noalloc(left_dev_ptr: int, n_left: int, right_dev_ptr: int, n_right: int, out_dev_ptr: int,

@@ -267,6 +267,10 @@ SJBG_API int sjbg_stream_close(sjbg_handle *h, sjbg_stream_stats *stats);
 SJBG_API int sjbg_generate(sjbg_handle *h, sjbg_tuple *dev_out, uint64_t first, uint64_t n,
                   uint64_t seed, uint64_t domain, const uint64_t *zipf_table, uint64_t perm_seed);
 
+/* Host-only helper of sjbg_generate: fill table[0..n) with the Zipf(z) CDF over
+ * ranks 0..n-1 in 64-bit fixed point (the layout sjbg_generate expects). */
+SJBG_API int sjbg_zipf_table(uint64_t *table, uint64_t n, double z);
+
 /* ---- allocation-free lazy hash join ------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a host framework that owns every device allocation, or a
