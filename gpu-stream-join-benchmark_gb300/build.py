@@ -82,8 +82,12 @@ def build_harness(force: bool = False) -> str | None:
     if not force and _newer(HARNESS, deps):
         return HARNESS
     cxx = shutil.which("g++") or "g++"
-    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", HOST] + srcs + [
-        "-o", HARNESS, "-L", LIBDIR, "-lsjbg", "-Wl,-rpath,$ORIGIN", "-lpthread"]
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    cudalib = os.path.join(cuda, "lib64")
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", HOST,
+           "-I", os.path.join(cuda, "include")] + srcs + [
+        "-o", HARNESS, "-L", LIBDIR, "-lsjbg", "-Wl,-rpath,$ORIGIN", "-L", cudalib, "-lcudart",
+        "-Wl,-rpath," + cudalib, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"harness build failed:\n{r.stdout}\n{r.stderr}")

@@ -771,6 +771,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
     const uint32_t tiles = tileL[n] + tileR[n];
     if (tiles) {
+        allow_big_smem(part_hist_kernel, sizeof(uint32_t) * maxP);
         SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(hgL[n] + hgR[n]), dim3(kPartThreads),
                           sizeof(uint32_t) * maxP, dL, dR, dPlan, n, dTileL, dTileR, dHgL, dHgR, dCnt, (uint32_t)B,
                           dModels, dHeavy));
@@ -885,6 +886,7 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
     const uint32_t *tl = rs->tile;
     if (tL + tR) {
         const uint32_t groups = (tL + kHistTiles - 1) / kHistTiles + (tR + kHistTiles - 1) / kHistTiles;
+        allow_big_smem(part_hist_kernel, sizeof(uint32_t) * P);
         part_hist_kernel<<<groups, kPartThreads, sizeof(uint32_t) * P, st>>>(
             dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr);
         part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);

@@ -42,7 +42,7 @@ template <bool kEnum, bool kPairs>
 __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uint32_t nL,
                                           const sjbg_tuple *__restrict__ Rw, uint32_t nR, uint32_t l0, uint32_t r0,
                                           WinAcc *acc, unsigned long long *extra_count, sjbg_pair *pout,
-                                          uint64_t pcap) {
+                                          uint64_t pcap, uint32_t rsplit = kRSplit) {
     __shared__ __align__(16) uint32_t rkeys[kChunk];
     __shared__ __align__(16) uint32_t rvals[kChunk];
     uint32_t lk[kLReg], lv[kLReg];
@@ -64,7 +64,7 @@ __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uin
         if (!((lvalid >> a) & 1u)) { lk[a] = fill; lv[a] = 0; }   // invalid slots only cause false alarms
 
     unsigned long long count = 0, xr = 0, prod = 0;
-    const uint32_t r_end = min(nR, r0 + kRSplit);
+    const uint32_t r_end = min(nR, r0 + rsplit);
     for (uint32_t c0 = r0; c0 < r_end; c0 += kChunk) {
         const uint32_t m = min(kChunk, r_end - c0);
         const uint32_t mpad = (m + kVote - 1) / kVote * kVote;
@@ -148,24 +148,28 @@ nlj_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, c
 template <bool kEnum, bool kPairs>
 __global__ void __launch_bounds__(kNljThreads)
 nlj_pair_kernel(const sjbg_tuple *__restrict__ L, uint32_t nL, const sjbg_tuple *__restrict__ R, uint32_t nR,
-                WinAcc *acc, unsigned long long *batch_count, sjbg_pair *pairs, uint64_t pairs_cap) {
-    nlj_block<kEnum, kPairs>(L, nL, R, nR, blockIdx.x * kLTile, blockIdx.y * kRSplit, acc, batch_count, pairs,
-                             pairs_cap);
+                uint32_t rsplit, WinAcc *acc, unsigned long long *batch_count, sjbg_pair *pairs, uint64_t pairs_cap) {
+    nlj_block<kEnum, kPairs>(L, nL, R, nR, blockIdx.x * kLTile, blockIdx.y * rsplit, acc, batch_count, pairs,
+                             pairs_cap, rsplit);
 }
 
 int nlj_pair_launch(sjbg_handle *h, const sjbg_tuple *L, uint64_t nL, const sjbg_tuple *R, uint64_t nR, WinAcc *acc,
                     unsigned long long *batch_count, sjbg_pair *pairs, uint64_t pairs_cap, bool enumerate) {
     if (nL == 0 || nR == 0) return SJBG_OK;
-    const dim3 grid((uint32_t)((nL + kLTile - 1) / kLTile), (uint32_t)((nR + kRSplit - 1) / kRSplit));
+    // split the right side finely enough that the grid covers every SM twice
+    const uint32_t lt = (uint32_t)((nL + kLTile - 1) / kLTile);
+    uint32_t rsplit = kRSplit;
+    while (rsplit > kChunk && (uint64_t)lt * ((nR + rsplit - 1) / rsplit) < 2ull * h->num_sms) rsplit >>= 1;
+    const dim3 grid(lt, (uint32_t)((nR + rsplit - 1) / rsplit));
     if (pairs)
         SJBG_CK(h, launch(h, "eager_nlj_pairs", nlj_pair_kernel<true, true>, grid, dim3(kNljThreads), 0, L,
-                          (uint32_t)nL, R, (uint32_t)nR, acc, batch_count, pairs, pairs_cap));
+                          (uint32_t)nL, R, (uint32_t)nR, rsplit, acc, batch_count, pairs, pairs_cap));
     else if (enumerate)
         SJBG_CK(h, launch(h, "eager_nlj_xor", nlj_pair_kernel<true, false>, grid, dim3(kNljThreads), 0, L,
-                          (uint32_t)nL, R, (uint32_t)nR, acc, batch_count, pairs, pairs_cap));
+                          (uint32_t)nL, R, (uint32_t)nR, rsplit, acc, batch_count, pairs, pairs_cap));
     else
         SJBG_CK(h, launch(h, "eager_nlj_count", nlj_pair_kernel<false, false>, grid, dim3(kNljThreads), 0, L,
-                          (uint32_t)nL, R, (uint32_t)nR, acc, batch_count, pairs, pairs_cap));
+                          (uint32_t)nL, R, (uint32_t)nR, rsplit, acc, batch_count, pairs, pairs_cap));
     return SJBG_OK;
 }
 

@@ -38,6 +38,15 @@ def lib():
 
 
 @pytest.fixture(scope="session")
+def harness():
+    """Path of the C++ runExperiment harness, built in-tree over the library."""
+    import build as b
+
+    b.build_lib()
+    return b.build_harness()
+
+
+@pytest.fixture(scope="session")
 def golden():
     import json
 

@@ -1,0 +1,85 @@
+"""GPU tests of the C++ host harness end to end: runExperiment generates both
+streams, feeds them batch by batch through the reference's windowing
+(lazy ring buffer / eager close rule) into the GPU joiners, and its match count,
+product checksum and per-batch progress equal the oracle's on the same
+streams."""
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 1 << 18            # tuples per stream
+W = 1 << 16            # windowSizesMB: [1]
+B = 1 << 13            # batchSizeKB: [128]
+DISTINCT = 1000
+
+
+def run(harness, tmp_path, alg, prog, result="NoOutput", theta="0.0", distinct=DISTINCT):
+    y = tmp_path / "exp.yaml"
+    y.write_text(
+        f'algTypes: [ "{alg}" ]\ndeviceTypes: [ "GPU" ]\nprogressivenessModes: [ "{prog}" ]\n'
+        f"distinctKeys: [ {distinct} ]\nzipfThetas: [ {theta} ]\nresultMaterializationMethod: [ \"{result}\" ]\n"
+        f'windowSizesMB: [ 1 ]\nbatchSizeKB: [ 128 ]\nmeasuredMetric: "cumulativePercentage"\n'
+        f'measurePowerUsage: "No"\nrepeat: 1\nparStrats: [ "INTRA" ]\ndataSize: {N}\nsourceThreads: 1\n')
+    r = subprocess.run([harness, str(y), str(tmp_path / "out.csv")], capture_output=True, text=True,
+                       cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    m = re.search(r"Match Count: (\d+)", r.stdout)
+    p = re.search(r"Prod checksum: (\d+)", r.stdout)
+    w = re.search(r"Windows: (\d+)", r.stdout)
+    rows = (tmp_path / "progressiveness.csv").read_text().strip().splitlines()[1:]
+    progress = [int(row.split(",")[4]) for row in rows]
+    return int(m.group(1)), int(p.group(1)), int(w.group(1)), progress
+
+
+def streams(oracle, theta=0.0, distinct=DISTINCT):
+    """The harness's streams: seeds 123 / 456, val = key, STEADY timestamps."""
+    out = []
+    for seed in (123, 456):
+        if theta > 0:
+            t = oracle.gen_zipf(0, N, seed, oracle.zipf_table(distinct, float(np.float32(theta))), distinct, 3)
+        else:
+            t = oracle.gen_uniform(0, N, seed, distinct)
+        t["val"] = t["key"]
+        t["ts"] = np.floor(np.arange(N) / np.floor(N / 1000)).astype(np.uint64)
+        out.append(t)
+    return out
+
+
+@pytest.mark.parametrize("alg,result", [("HJ", "NoOutput"), ("HJ", "Atomic"), ("SMJ", "NoOutput"),
+                                        ("NLJ", "CountKernel")])
+def test_lazy_harness_matches_oracle(harness, oracle, tmp_path, alg, result):
+    left, right = streams(oracle)
+    count, prod, windows, progress = run(harness, tmp_path, alg, "LAZY", result)
+    want_c = want_p = 0
+    cum = []
+    for k in range(N // W):
+        r = oracle.join(left[k * W:(k + 1) * W], right[k * W:(k + 1) * W], enumerate_pairs=False)
+        want_c += r["count"]
+        want_p = (want_p + r["prod"]) % (1 << 64)
+        cum.append(want_c)
+    assert windows == N // W
+    assert (count, prod) == (want_c, want_p)
+    assert progress == cum
+
+
+def test_lazy_harness_zipf(harness, oracle, tmp_path):
+    left, right = streams(oracle, theta=0.9, distinct=1 << 16)
+    count, prod, _, _ = run(harness, tmp_path, "HJ", "LAZY", theta="0.9", distinct=1 << 16)
+    want = [oracle.join(left[k * W:(k + 1) * W], right[k * W:(k + 1) * W], enumerate_pairs=False)
+            for k in range(N // W)]
+    assert count == sum(r["count"] for r in want)
+    assert prod == sum(r["prod"] for r in want) % (1 << 64)
+
+
+@pytest.mark.parametrize("alg", ["HJ", "NLJ"])
+def test_eager_harness_matches_oracle(harness, oracle, tmp_path, alg):
+    left, right = streams(oracle)
+    count, _, windows, progress = run(harness, tmp_path, alg, "EAGER")
+    bc, wc = oracle.eager_hj(left, right, B, W, DISTINCT)
+    assert count == int(bc.sum())
+    assert progress == np.cumsum(bc).tolist()          # one progress record per batch, arrival order
+    assert windows == len(wc) - 1                      # closes counted; the last window stays open
