@@ -34,6 +34,7 @@ sjbg_handle::~sjbg_handle() {
     }
     for (auto e : event_pool) cudaEventDestroy(e);
     if (own_stream) cudaStreamDestroy(own_stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
 }
 
 namespace sjbg {
@@ -96,6 +97,28 @@ void *pinned_get(sjbg_handle *h, int i, size_t bytes) {
     return b.p;
 }
 
+// Small staging transfers (plans, accumulators) between pinned host memory
+// and device memory are done by a kernel over mapped pinned memory, not by a
+// copy engine: a copy engine works its queue in order, so a plan upload
+// queued behind a large input copy on another stream would wait for it.
+__global__ void stage_copy_kernel(uint8_t *__restrict__ dst, const uint8_t *__restrict__ src, size_t bytes,
+                                  bool vec) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t n16 = vec ? bytes / 16 : 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += stride)
+        reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+    for (size_t i = n16 * 16 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < bytes; i += stride) dst[i] = src[i];
+}
+
+int stage_copy(sjbg_handle *h, void *dst, const void *src, size_t bytes) {
+    if (bytes == 0) return SJBG_OK;
+    const bool vec = (((uintptr_t)dst | (uintptr_t)src) & 15u) == 0;
+    const uint32_t blocks = (uint32_t)std::min<size_t>(64, (bytes + 4095) / 4096);
+    SJBG_CK(h, launch(h, "stage_copy", stage_copy_kernel, dim3(blocks), dim3(256), 0, static_cast<uint8_t *>(dst),
+                      static_cast<const uint8_t *>(src), bytes, vec));
+    return SJBG_OK;
+}
+
 int kernel_id(sjbg_handle *h, const char *name) {
     for (size_t i = 0; i < h->knames.size(); i++)
         if (h->knames[i] == name) return (int)i;
@@ -137,9 +160,10 @@ int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
                            sjbg_pair *dPairs, WinAcc *hAcc, uint32_t *part_used) {
     const bool pairs = dPairs != nullptr;
     const bool enumerate = pairs || (h->cfg.flags & SJBG_F_XOR);
-    WinAcc *acc = static_cast<WinAcc *>(ws_get(h, WS_WIN_ACC, sizeof(WinAcc) * n));
+    // acc[n].info is the call's device status word (kErr* bits)
+    WinAcc *acc = static_cast<WinAcc *>(ws_get(h, WS_WIN_ACC, sizeof(WinAcc) * (n + 1)));
     if (!acc) return fail(h, SJBG_E_NOMEM, "window accumulators");
-    SJBG_CK(h, cudaMemsetAsync(acc, 0, sizeof(WinAcc) * n, h->stream));
+    SJBG_CK(h, cudaMemsetAsync(acc, 0, sizeof(WinAcc) * (n + 1), h->stream));
     int rc = SJBG_OK;
     *part_used = SJBG_PART_NONE;
     switch (h->cfg.algorithm) {
@@ -149,8 +173,15 @@ int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         default: rc = fail(h, SJBG_E_UNSUPPORTED, "unknown algorithm");
     }
     if (rc) return rc;
-    SJBG_CK(h, cudaMemcpyAsync(hAcc, acc, sizeof(WinAcc) * n, cudaMemcpyDeviceToHost, h->stream));
-    return SJBG_OK;
+    return stage_copy(h, hAcc, acc, sizeof(WinAcc) * (n + 1));
+}
+
+int device_status_error(sjbg_handle *h, unsigned long long bits) {
+    if (!bits) return SJBG_OK;
+    if (bits & kErrTimeout) return fail(h, SJBG_E_TIMEOUT, "a bounded device-side wait gave up");
+    if (bits & kErrTableFull) return fail(h, SJBG_E_CAPACITY, "a device hash table could not take a key");
+    if (bits & kErrQueue) return fail(h, SJBG_E_CAPACITY, "a device work queue overflowed");
+    return fail(h, SJBG_E_INVALID, "a kernel rejected a window descriptor");
 }
 
 static void fill_result(const sjbg_handle *h, const WinAcc &a, const WinHost &w, bool enumerate, bool pairs,
@@ -201,7 +232,7 @@ static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR
         hAcc = static_cast<WinAcc *>(entry->pinned[3].p);
         part_used = entry->part_used;
     } else {
-        hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * std::max<uint32_t>(n, 1)));
+        hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * (n + 1)));
         if (!hAcc) return fail(h, SJBG_E_NOMEM, "result staging");
         SJBG_CK(h, cudaEventRecord(e0, h->stream));
         int rc = run_lazy_device(h, dL, dR, wins, n, dPairs, hAcc, &part_used);   // warm-up: sizes every buffer
@@ -257,7 +288,111 @@ static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR
     cudaEventElapsedTime(&ms, e0, e1);
     h->event_pool.push_back(e0);
     h->event_pool.push_back(e1);
+    if (int se = device_status_error(h, hAcc[n].info)) return se;
     for (uint32_t w = 0; w < n; w++) fill_result(h, hAcc[w], wins[w], enumerate, dPairs != nullptr, part_used, ms, &out[w]);
+    return SJBG_OK;
+}
+
+// Host inputs, several windows: the windows are cut into groups of about an
+// eighth of the input bytes; every group's input copy is enqueued at once on
+// the copy stream, and each group's join starts as soon as its copy has
+// landed, so the joins of early groups overlap the copies of later ones.
+// The groups run one after another on the handle's stream (the staging
+// buffers are reused), so the call lasts about the copy time plus the last
+// group's join.
+static int lazy_host_pipelined(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, const WinHost *wins,
+                               uint32_t n, sjbg_pair *pairs, bool want, bool enumerate, uint64_t needL,
+                               uint64_t needR, uint64_t needP, sjbg_window_result *out) {
+    if (!h->copy_stream) SJBG_CK(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    sjbg_tuple *sL = static_cast<sjbg_tuple *>(ws_get(h, WS_IN_LEFT, sizeof(sjbg_tuple) * needL));
+    sjbg_tuple *sR = static_cast<sjbg_tuple *>(ws_get(h, WS_IN_RIGHT, sizeof(sjbg_tuple) * needR));
+    sjbg_pair *dP = want ? static_cast<sjbg_pair *>(ws_get(h, WS_PAIRS, sizeof(sjbg_pair) * needP)) : nullptr;
+    if ((needL && !sL) || (needR && !sR) || (want && !dP)) return fail(h, SJBG_E_NOMEM, "input staging");
+    uint64_t total = 0;
+    for (uint32_t w = 0; w < n; w++) total += wins[w].n_left + wins[w].n_right;
+    std::vector<uint32_t> gfirst;   // first window of each group
+    uint64_t run = 0;
+    for (uint32_t w = 0; w < n; w++) {
+        if (w == 0 || run >= total / 8) {
+            gfirst.push_back(w);
+            run = 0;
+        }
+        run += wins[w].n_left + wins[w].n_right;
+    }
+    const uint32_t G = (uint32_t)gfirst.size();
+    gfirst.push_back(n);
+    std::vector<cudaEvent_t> landed(G);
+    for (auto &e : landed) e = event_get(h);
+    cudaEvent_t e0 = event_get(h), e1 = event_get(h);
+    auto release = [&]() {
+        for (auto e : landed) h->event_pool.push_back(e);
+        h->event_pool.push_back(e0);
+        h->event_pool.push_back(e1);
+    };
+    SJBG_CK(h, cudaEventRecord(e0, h->stream));
+    SJBG_CK(h, cudaStreamWaitEvent(h->copy_stream, e0, 0));
+    for (uint32_t g = 0; g < G; g++) {
+        uint64_t lo[2] = {~0ull, ~0ull}, hi[2] = {0, 0};
+        for (uint32_t w = gfirst[g]; w < gfirst[g + 1]; w++) {
+            if (wins[w].n_left) {
+                lo[0] = std::min(lo[0], wins[w].left_off);
+                hi[0] = std::max(hi[0], wins[w].left_off + wins[w].n_left);
+            }
+            if (wins[w].n_right) {
+                lo[1] = std::min(lo[1], wins[w].right_off);
+                hi[1] = std::max(hi[1], wins[w].right_off + wins[w].n_right);
+            }
+        }
+        if (hi[0] > lo[0] && lo[0] != ~0ull)
+            SJBG_CK(h, cudaMemcpyAsync(sL + lo[0], L + lo[0], sizeof(sjbg_tuple) * (hi[0] - lo[0]),
+                                       cudaMemcpyHostToDevice, h->copy_stream));
+        if (hi[1] > lo[1] && lo[1] != ~0ull)
+            SJBG_CK(h, cudaMemcpyAsync(sR + lo[1], R + lo[1], sizeof(sjbg_tuple) * (hi[1] - lo[1]),
+                                       cudaMemcpyHostToDevice, h->copy_stream));
+        SJBG_CK(h, cudaEventRecord(landed[g], h->copy_stream));
+    }
+    std::vector<WinAcc> acc(n);
+    uint32_t part_used = SJBG_PART_NONE;
+    for (uint32_t g = 0; g < G; g++) {
+        const uint32_t w0 = gfirst[g], m = gfirst[g + 1] - w0;
+        WinAcc *hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * (m + 1)));
+        if (!hAcc) {
+            release();
+            return fail(h, SJBG_E_NOMEM, "result staging");
+        }
+        SJBG_CK(h, cudaStreamWaitEvent(h->stream, landed[g], 0));
+        uint32_t pu = SJBG_PART_NONE;
+        int rc = run_lazy_device(h, sL, sR, wins + w0, m, dP, hAcc, &pu);
+        if (rc) {
+            cudaStreamSynchronize(h->copy_stream);
+            release();
+            return rc;
+        }
+        if (g == 0) part_used = pu;
+        // the staging buffers (pinned plan uploads, accumulators) are reused by the next group
+        SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        if (int se = device_status_error(h, hAcc[m].info)) {
+            cudaStreamSynchronize(h->copy_stream);
+            release();
+            return se;
+        }
+        std::copy(hAcc, hAcc + m, acc.begin() + w0);
+    }
+    if (want) {
+        for (uint32_t w = 0; w < n; w++) {
+            const uint64_t np = std::min<uint64_t>(acc[w].npairs, wins[w].pairs_cap);
+            if (np)
+                SJBG_CK(h, cudaMemcpyAsync(pairs + wins[w].pairs_off, dP + wins[w].pairs_off, sizeof(sjbg_pair) * np,
+                                           cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    SJBG_CK(h, cudaEventRecord(e1, h->stream));
+    SJBG_CK(h, cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    release();
+    profile_collect(h);
+    for (uint32_t w = 0; w < n; w++) fill_result(h, acc[w], wins[w], enumerate, want, part_used, ms, &out[w]);
     return SJBG_OK;
 }
 
@@ -289,6 +424,8 @@ int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32
     }
     if ((h->cfg.flags & SJBG_F_GRAPH) && mem == SJBG_MEM_DEVICE && h->cfg.result_mode != SJBG_RESULT_COUNT_KERNEL)
         return lazy_graph(h, L, R, wins, n, want ? pairs : nullptr, enumerate, out);
+    if (mem == SJBG_MEM_HOST && n > 1 && !(want && h->cfg.result_mode == SJBG_RESULT_COUNT_KERNEL))
+        return lazy_host_pipelined(h, L, R, wins, n, pairs, want, enumerate, needL, needR, needP, out);
     cudaEvent_t e0 = event_get(h), e1 = event_get(h);
     SJBG_CK(h, cudaEventRecord(e0, h->stream));
     const sjbg_tuple *dL = L, *dR = R;
@@ -308,17 +445,18 @@ int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32
     }
     // CountKernel mode: an exact count first; refuse instead of truncating
     if (want && h->cfg.result_mode == SJBG_RESULT_COUNT_KERNEL) {
-        WinAcc *hp = static_cast<WinAcc *>(pinned_get(h, 4, sizeof(WinAcc) * n));
+        WinAcc *hp = static_cast<WinAcc *>(pinned_get(h, 4, sizeof(WinAcc) * (n + 1)));
         if (!hp) return fail(h, SJBG_E_NOMEM, "count staging");
         uint32_t pu;
         int rc = run_lazy_device(h, dL, dR, wins, n, nullptr, hp, &pu);
         if (rc) return rc;
         SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        if (int se = device_status_error(h, hp[n].info)) return se;
         for (uint32_t w = 0; w < n; w++)
             if (hp[w].count > wins[w].pairs_cap)
                 return fail(h, SJBG_E_CAPACITY, "pair buffer smaller than the window's match count");
     }
-    WinAcc *hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * std::max<uint32_t>(n, 1)));
+    WinAcc *hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * (n + 1)));
     if (!hAcc) return fail(h, SJBG_E_NOMEM, "result staging");
     uint32_t part_used = SJBG_PART_NONE;
     int rc = run_lazy_device(h, dL, dR, wins, n, dP, hAcc, &part_used);
@@ -326,6 +464,7 @@ int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32
     if (mem == SJBG_MEM_HOST && want) {
         // copy back each window's written pairs
         SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        if (int se = device_status_error(h, hAcc[n].info)) return se;
         for (uint32_t w = 0; w < n; w++) {
             const uint64_t np = std::min<uint64_t>(hAcc[w].npairs, wins[w].pairs_cap);
             if (np)
@@ -340,6 +479,7 @@ int lazy_common(sjbg_handle *h, const sjbg_tuple *L, const sjbg_tuple *R, uint32
     h->event_pool.push_back(e0);
     h->event_pool.push_back(e1);
     profile_collect(h);
+    if (int se = device_status_error(h, hAcc[n].info)) return se;
     for (uint32_t w = 0; w < n; w++) fill_result(h, hAcc[w], wins[w], enumerate, want, part_used, ms, &out[w]);
     return SJBG_OK;
 }

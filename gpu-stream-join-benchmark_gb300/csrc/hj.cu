@@ -52,19 +52,29 @@ __device__ __forceinline__ uint32_t find_window(const uint32_t *prefix, uint32_t
 
 // Partitioning model of the CTA's window: learned (when it has a model that
 // did not fall back) or plain radix on the key's low bits.
+// The CTA's copy of the model lives in shared memory (`core`).
 struct Classifier {
-    const LearnedModel *m;   // null: radix
+    const LearnedCore *m;   // null: radix
     uint32_t mask;
     __device__ __forceinline__ uint32_t bucket(uint32_t key) const {
         return m ? learned_bucket(*m, key) : (key & mask);
     }
 };
 
-__device__ __forceinline__ Classifier make_classifier(const WinPlan &wp, const LearnedModel *models) {
+// The window's model in global memory, or null for radix partitioning.
+__device__ __forceinline__ const LearnedModel *model_of(const WinPlan &wp, const LearnedModel *models) {
+    return (wp.model != 0xFFFFFFFFu && !models[wp.model].fallback) ? &models[wp.model] : nullptr;
+}
+
+// All threads of the CTA; ends with a barrier when the window has a model.
+__device__ __forceinline__ Classifier make_classifier(const WinPlan &wp, const LearnedModel *gm, LearnedCore &core) {
     Classifier c;
     c.m = nullptr;
-    if (wp.model != 0xFFFFFFFFu && !models[wp.model].fallback) c.m = &models[wp.model];
     c.mask = (1u << wp.log2_buckets) - 1u;
+    if (gm) {
+        copy_to_smem(&core, gm, sizeof(LearnedCore));
+        c.m = &core;
+    }
     return c;
 }
 
@@ -96,16 +106,18 @@ __device__ __forceinline__ bool warp_group(bool valid, uint32_t tag, unsigned lo
 // ------------------------------------------------------------------ 1. histogram
 // Also aggregates heavy keys of learned windows: per heavy key, count and
 // sum of fr (left) / gs (right); heavy tuples are not partitioned.
-__global__ void __launch_bounds__(kPartThreads)
+__global__ void __launch_bounds__(kPartThreads, 2)
 part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                  uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
                  const uint32_t *__restrict__ hgroupL, const uint32_t *__restrict__ hgroupR,
                  uint32_t *__restrict__ cnt, uint32_t B, const LearnedModel *__restrict__ models,
-                 HeavyAcc *__restrict__ hacc) {
+                 HeavyAcc *__restrict__ hacc, uint64_t *__restrict__ compL, uint64_t *__restrict__ compR,
+                 uint32_t *__restrict__ ccnt) {
     extern __shared__ uint32_t hist[];
     __shared__ HeavySet hs;
     __shared__ uint32_t hcnt[kMaxHeavy];
     __shared__ unsigned long long hsum[kMaxHeavy];
+    __shared__ uint32_t cwarp[2][32], cbase[2];   // light-tuple compaction, double-buffered by tile
     // this CTA covers tiles [t, t + kHistTiles) of one window side ("hist groups")
     const bool right = blockIdx.x >= hgroupL[nwin];
     const uint32_t g = right ? blockIdx.x - hgroupL[nwin] : blockIdx.x;
@@ -113,8 +125,13 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     const uint32_t *tp = right ? tileR : tileL;
     const uint32_t w = find_window(hp, nwin, g);
     const WinPlan wp = wins[w];
-    const Classifier cls = make_classifier(wp, models);
+    __shared__ LearnedCore core;
+    const LearnedModel *gm = model_of(wp, models);
+    const Classifier cls = make_classifier(wp, gm, core);
     const bool heavy = cls.m && cls.m->n_heavy;
+    const bool compact = heavy && cls.m->compact;
+    // compact arrays: window w's side starts at its first tile * kTile
+    uint64_t *cdst = compact ? (right ? compR : compL) + (uint64_t)tp[w] * kTile : nullptr;
     const uint64_t nside = right ? wp.n_right : wp.n_left;
     const uint32_t t_first = (g - hp[w]) * kHistTiles;            // tile index inside the window
     const uint32_t t_end = min(t_first + kHistTiles, tp[w + 1] - tp[w]);
@@ -122,7 +139,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
     if (heavy) {
         for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum[i] = 0; }
-        heavy_set_load(hs, cls.m);   // ends with a barrier
+        heavy_set_load(hs, gm);   // ends with a barrier
     }
     SJBG_BARRIER();
     // the hottest heavy keys (the fit orders heavy keys by sampled count) are
@@ -131,16 +148,30 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     uint32_t rc[kRegHeavy] = {0, 0, 0, 0};
     unsigned long long rs[kRegHeavy] = {0, 0, 0, 0};
     constexpr int kPer = kTile / kPartThreads;
+    const sjbg_tuple *base = right ? R + wp.right_off : L + wp.left_off;
+    // key and val of the thread's tuples of tile tt (the sectors read are those
+    // of whole tuples, the registers half)
+    auto load_tile = [&](uint32_t tt, uint2 (&v)[kPer]) {
+        const uint64_t start = (uint64_t)tt * kTile;
+        const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+        const uint2 *src = reinterpret_cast<const uint2 *>(base + start);
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const uint32_t i = threadIdx.x + k * kPartThreads;
+            v[k] = i < n ? __ldg(src + 2 * i) : make_uint2(0u, 0u);
+        }
+    };
+    // software pipeline: tile tt+1 is in flight while tile tt is counted
+    uint2 nv[kPer];
+    if (t_first < t_end) load_tile(t_first, nv);
     for (uint32_t tt = t_first; tt < t_end; tt++) {
     const uint64_t start = (uint64_t)tt * kTile;
     const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
-    const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
-    uint4 v[kPer];
+    uint2 v[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {   // all of the thread's loads in flight before any use
-        const uint32_t i = threadIdx.x + k * kPartThreads;
-        v[k] = i < n ? __ldg(src + i) : make_uint4(0u, 0u, 0u, 0u);   // whole 16-byte tuple
-    }
+    for (int k = 0; k < kPer; k++) v[k] = nv[k];
+    if (tt + 1 < t_end) load_tile(tt + 1, nv);
+    uint32_t lightmask = 0;
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
         const uint32_t i = threadIdx.x + k * kPartThreads;
@@ -160,6 +191,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                 }
             } else if (valid) {
                 atomicAdd(&hist[cls.bucket(key)], 1u);   // light keys: balanced buckets
+                lightmask |= 1u << k;
             }
         } else {
             // plain partitioning: skewed keys hammer one bucket, so equal buckets
@@ -169,6 +201,28 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const uint32_t b = valid ? cls.bucket(key) : 0u;
             if (warp_group(valid, b, 0ull, false, &gs, &gsum)) atomicAdd(&hist[b], gs);
         }
+    }
+    if (compact) {
+        // the tile's light tuples go to the window side's compact array as
+        // (key,val) words: warp scan, block scan, one global reservation
+        const uint32_t par = tt & 1u;
+        const uint32_t nl = __popc(lightmask);
+        uint32_t wt;
+        const uint32_t ex = warp_excl_scan(nl, &wt);
+        if (lane_id() == 31) cwarp[par][warp_id()] = ex + nl;
+        SJBG_BARRIER();
+        if (warp_id() == 0) {
+            const uint32_t x = lane_id() < (blockDim.x >> 5) ? cwarp[par][lane_id()] : 0u;
+            uint32_t tot;
+            const uint32_t e = warp_excl_scan(x, &tot);
+            cwarp[par][lane_id()] = e;
+            if (lane_id() == 0) cbase[par] = tot ? atomicAdd(&ccnt[2 * w + (right ? 1 : 0)], tot) : 0u;
+        }
+        SJBG_BARRIER();
+        uint32_t pos = cbase[par] + cwarp[par][warp_id()] + ex;
+#pragma unroll
+        for (int k = 0; k < kPer; k++)
+            if ((lightmask >> k) & 1u) cdst[pos++] = ((uint64_t)v[k].y << 32) | v[k].x;
     }
     }
     if (heavy) {
@@ -297,11 +351,12 @@ __device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
 }
 
 // ------------------------------------------------------------------ 3. scatter
-__global__ void __launch_bounds__(kPartThreads)
+__global__ void __launch_bounds__(kPartThreads, 3)
 part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                     uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
                     uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
-                    const LearnedModel *__restrict__ models) {
+                    const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
+                    const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t warp_tot[32];
     const uint32_t tilesL = tileL[nwin];
@@ -310,24 +365,30 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
     const uint32_t *tp = right ? tileR : tileL;
     const uint32_t w = find_window(tp, nwin, t);
     const WinPlan wp = wins[w];
-    const uint64_t nside = right ? wp.n_right : wp.n_left;
+    const LearnedModel *gm = model_of(wp, models);
+    // compacted windows: the tiles cover the light tuples the counting pass wrote out
+    const bool compact = gm && gm->n_heavy && gm->compact;
+    const uint64_t nside = compact ? ccnt[2 * w + (right ? 1 : 0)] : (right ? wp.n_right : wp.n_left);
     const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
+    if (start >= nside) return;   // whole CTA
     const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
     const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
+    const uint64_t *csrc = compact ? (right ? compR : compL) + (uint64_t)tp[w] * kTile + start : nullptr;
     const uint32_t P = 1u << wp.log2_buckets;
 
     uint64_t *stage = reinterpret_cast<uint64_t *>(smem_raw);                  // kTile
     uint16_t *sb = reinterpret_cast<uint16_t *>(stage + kTile);                // kTile bucket ids
     uint32_t *lcnt = reinterpret_cast<uint32_t *>(sb + kTile);                 // P
     uint32_t *gbase = lcnt + P;                                                // P
-    const Classifier cls = make_classifier(wp, models);
-    const bool heavy = cls.m && cls.m->n_heavy;
+    __shared__ LearnedCore core;
+    const Classifier cls = make_classifier(wp, gm, core);
+    const bool heavy = cls.m && cls.m->n_heavy && !compact;
     __shared__ HeavySet hs;
     __shared__ uint32_t kept_s;
 
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) lcnt[i] = 0;
     if (threadIdx.x == 0) kept_s = 0;
-    if (heavy) heavy_set_load(hs, cls.m);
+    if (heavy) heavy_set_load(hs, gm);
     SJBG_BARRIER();
     constexpr int kPer = kTile / kPartThreads;
     uint64_t e[kPer];
@@ -336,8 +397,12 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
     for (int k = 0; k < kPer; k++) {   // all of the thread's loads in flight before any use
         const uint32_t i = threadIdx.x + k * kPartThreads;
         if (i < n) {
-            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(src + i));   // key and val only
-            e[k] = ((uint64_t)v.y << 32) | v.x;
+            if (compact) {
+                e[k] = __ldg(csrc + i);
+            } else {
+                const uint2 v = __ldg(reinterpret_cast<const uint2 *>(src + i));   // key and val only
+                e[k] = ((uint64_t)v.y << 32) | v.x;
+            }
         }
     }
 #pragma unroll
@@ -468,12 +533,16 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
     if (nR == 0 || nS == 0) return;
     uint64_t *Rb = partL + start[b];
     const uint64_t *Sb = partR + start[B + b];
-    const uint32_t C = 1u << table_bits;
+    // the table holds at most nR distinct keys: twice that many slots (at
+    // least 64, at most the launch's table) keep small buckets cheap to clear
+    uint32_t bits = 6;
+    while (bits < table_bits && (1u << bits) < 2 * nR) bits++;
+    const uint32_t C = 1u << bits;
     CountTable t;
     t.sumf = reinterpret_cast<unsigned long long *>(smem_raw);
     t.keys = reinterpret_cast<uint32_t *>(t.sumf + C + 1);
     t.cnt = t.keys + C + 1;
-    t.bits = table_bits;
+    t.bits = bits;
     const uint32_t tile = kJoinPer * blockDim.x;
 
     unsigned long long count = 0, prod = 0;
@@ -547,10 +616,10 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
     const uint64_t *Rb = partL + start[b];
     const uint64_t *Sb = partR + start[B + b];
     const uint32_t w = bucket_win[b];
-    const uint32_t C = 1u << table_bits;
-    uint32_t *keys = reinterpret_cast<uint32_t *>(smem_raw);   // C + 1
-    uint32_t *head = keys + C + 1;                             // C + 1
-    uint32_t *next = head + C + 1;                             // kEnumChunk
+    const uint32_t Cmax = 1u << table_bits;
+    uint32_t *keys = reinterpret_cast<uint32_t *>(smem_raw);   // Cmax + 1
+    uint32_t *head = keys + Cmax + 1;                          // Cmax + 1
+    uint32_t *next = head + Cmax + 1;                          // kEnumChunk
     uint32_t *vals = next + kEnumChunk;                        // kEnumChunk
     const uint64_t pcap = pairs ? wins[w].pairs_cap : 0;
     sjbg_pair *pout = pairs ? pairs + wins[w].pairs_off : nullptr;
@@ -558,6 +627,10 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
     unsigned long long count = 0, prod = 0, xr = 0;
     for (uint32_t c0 = 0; c0 < nR; c0 += kEnumChunk) {
         const uint32_t m = min(kEnumChunk, nR - c0);
+        // at least twice as many slots as the chunk has tuples (slot C holds key 0xFFFFFFFF)
+        uint32_t bits = 6;
+        while (bits < table_bits && (1u << bits) < 2 * m) bits++;
+        const uint32_t C = 1u << bits;
         for (uint32_t i = threadIdx.x; i <= C; i += blockDim.x) {
             keys[i] = kEmptyKey;
             head[i] = kNil;
@@ -575,7 +648,7 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
                 if (key == kEmptyKey) {
                     s = C;
                 } else {
-                    s = slot_hash(key, table_bits);
+                    s = slot_hash(key, bits);
                     // at most m <= C/2 keys: a free or matching slot exists within C probes
                     for (uint32_t p = 0; p < C; p++) {
                         const uint32_t prev = atomicCAS(&keys[s], kEmptyKey, key);
@@ -600,7 +673,7 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
                 if (key == kEmptyKey) {
                     s = C;
                 } else {
-                    uint32_t q = slot_hash(key, table_bits);
+                    uint32_t q = slot_hash(key, bits);
                     for (uint32_t p = 0; p <= C; p++) {
                         const uint32_t k = keys[q];
                         if (k == key) { s = q; break; }
@@ -692,6 +765,10 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
                   sjbg_pair *dPairs, WinAcc *acc, bool enumerate, uint32_t *part_used) {
     if (n == 0) return SJBG_OK;
     const uint32_t part = h->cfg.partitioner;
+    if (part == SJBG_PART_NONE) {   // one HBM table per window (hj_global.cu)
+        if (part_used) *part_used = SJBG_PART_NONE;
+        return hj_global_batch(h, dL, dR, wins, n, dPairs, acc, enumerate);
+    }
     const bool learned = part == SJBG_PART_LEARNED;
     if (part_used) *part_used = learned ? SJBG_PART_LEARNED : SJBG_PART_RADIX;
     // left tuples per bucket: 2048 when chains are built, else the tuned target
@@ -743,7 +820,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     std::memcpy(hst + planB + 2 * tileB, hgL.data(), tileB);
     std::memcpy(hst + planB + 3 * tileB, hgR.data(), tileB);
     std::memcpy(hst + planB + 4 * tileB, bwin.data(), bwB);
-    SJBG_CK(h, cudaMemcpyAsync(dev, hst, upB, cudaMemcpyHostToDevice, h->stream));
+    if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
     WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
     const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
     const uint32_t *dTileR = reinterpret_cast<const uint32_t *>(dev + planB + tileB);
@@ -760,12 +837,21 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     const LearnedModel *dModels = nullptr;
     HeavyAcc *dHeavy = nullptr;
+    uint64_t *dComp = nullptr;
+    uint32_t *dCcnt = nullptr;
     if (learned) {
         int rc = learned_prepare(h, dL, dR, plan.data(), n, dPlan, &dModels, !enumerate);
         if (rc) return rc;
         dHeavy = static_cast<HeavyAcc *>(ws_get(h, WS_HEAVY, sizeof(HeavyAcc) * kMaxHeavy * n));
         if (!dHeavy) return fail(h, SJBG_E_NOMEM, "heavy-key accumulators");
         SJBG_CK(h, cudaMemsetAsync(dHeavy, 0, sizeof(HeavyAcc) * kMaxHeavy * n, h->stream));
+        if (!enumerate) {   // heavy keys exist only in count mode
+            dComp = static_cast<uint64_t *>(
+                ws_get(h, WS_COMPACT, sizeof(uint64_t) * kTile * ((uint64_t)tileL[n] + tileR[n])));
+            dCcnt = static_cast<uint32_t *>(ws_get(h, WS_COMPACT_CNT, sizeof(uint32_t) * 2 * n));
+            if (!dComp || !dCcnt) return fail(h, SJBG_E_NOMEM, "compaction buffers");
+            SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * 2 * n, h->stream));
+        }
     }
 
     SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
@@ -774,7 +860,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         allow_big_smem(part_hist_kernel, sizeof(uint32_t) * maxP);
         SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(hgL[n] + hgR[n]), dim3(kPartThreads),
                           sizeof(uint32_t) * maxP, dL, dR, dPlan, n, dTileL, dTileR, dHgL, dHgR, dCnt, (uint32_t)B,
-                          dModels, dHeavy));
+                          dModels, dHeavy, dComp, dComp ? dComp + (uint64_t)kTile * tileL[n] : nullptr, dCcnt));
         if (learned)
             SJBG_CK(h, launch(h, "heavy_finish", heavy_finish_kernel, dim3(n), dim3(256), 0, (const WinPlan *)dPlan, n,
                               dModels, (const HeavyAcc *)dHeavy, acc));
@@ -783,7 +869,9 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;
         allow_big_smem(part_scatter_kernel, scatterSmem);
         SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(tiles), dim3(kPartThreads), scatterSmem,
-                          dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels));
+                          dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels,
+                          (const uint64_t *)dComp, dComp ? (const uint64_t *)dComp + (uint64_t)kTile * tileL[n] : nullptr,
+                          (const uint32_t *)dCcnt));
     }
     // persistent CTAs draining a work queue of buckets, or one CTA per bucket
     uint32_t *queue = nullptr;
@@ -888,12 +976,12 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         const uint32_t groups = (tL + kHistTiles - 1) / kHistTiles + (tR + kHistTiles - 1) / kHistTiles;
         allow_big_smem(part_hist_kernel, sizeof(uint32_t) * P);
         part_hist_kernel<<<groups, kPartThreads, sizeof(uint32_t) * P, st>>>(
-            dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr);
+            dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr, nullptr, nullptr, nullptr);
         part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * P;
         allow_big_smem(part_scatter_kernel, scatterSmem);
         part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, cur, P, pL,
-                                                                          pR, nullptr);
+                                                                          pR, nullptr, nullptr, nullptr, nullptr);
         const uint32_t bits = 13;
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);

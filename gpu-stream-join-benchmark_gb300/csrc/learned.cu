@@ -42,7 +42,8 @@ struct SampleWin {
 struct SampleScratch {
     uint32_t kmin, kmax;   // sample key range
     uint32_t n_cand;
-    uint32_t pad;
+    uint32_t cut;          // candidates have a sample count >= cut
+    uint32_t cls[32];      // candidate keys per count class floor(log2(count))
 };
 
 __device__ __forceinline__ uint32_t sample_key(const SampleWin &s, const sjbg_tuple *L, const sjbg_tuple *R, uint32_t i) {
@@ -120,9 +121,9 @@ sample_count_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *w
     }
 }
 
+// Candidates per count class, so that the candidate cut keeps the heaviest keys.
 __global__ void __launch_bounds__(kSampleThreads)
-heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, SampleScratch *scr,
-                        unsigned long long *cand) {
+heavy_classes_kernel(const SampleWin *wins, const unsigned long long *table, SampleScratch *scr) {
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
     const unsigned long long *tw = table + s.table_off;
@@ -130,7 +131,34 @@ heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
         const unsigned long long v = tw[i];
         const uint32_t c = (uint32_t)v;
-        if (v && c >= s.thresh) {
+        if (v && c >= s.thresh) atomicAdd(&scr[w].cls[31 - __clz(c)], 1u);
+    }
+}
+
+// The smallest count class boundary 2^k (>= thresh) above which at most
+// kCandMax keys lie: every key counted more often than any dropped key is kept.
+__device__ __forceinline__ uint32_t candidate_cut(const SampleScratch &sc, uint32_t thresh) {
+    uint32_t acc = 0;
+    for (int k = 31; k >= 0; k--) {
+        acc += sc.cls[k];
+        if (acc > kCandMax) return max(thresh, k == 31 ? 0xFFFFFFFFu : (1u << (k + 1)));
+    }
+    return thresh;
+}
+
+__global__ void __launch_bounds__(kSampleThreads)
+heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, SampleScratch *scr,
+                        unsigned long long *cand) {
+    const uint32_t w = blockIdx.y;
+    const SampleWin s = wins[w];
+    const unsigned long long *tw = table + s.table_off;
+    const uint32_t slots = 1u << s.table_log2;
+    const uint32_t cut = candidate_cut(scr[w], s.thresh);
+    if (blockIdx.x == 0 && threadIdx.x == 0) scr[w].cut = cut;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
+        const unsigned long long v = tw[i];
+        const uint32_t c = (uint32_t)v;
+        if (v && c >= cut) {
             uint32_t pos = atomicAdd(&scr[w].n_cand, 1u);
             // candidates sort by count descending, then key: (count << 32 | ~key)
             if (pos < kCandMax) cand[(uint64_t)w * kCandMax + pos] = ((unsigned long long)c << 32) | (~(uint32_t)(v >> 32));
@@ -141,13 +169,13 @@ heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, 
 // One CTA (1024 threads) per window.
 __global__ void __launch_bounds__(1024)
 learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, unsigned long long *cand,
-                   LearnedModel *models, uint32_t leaves, uint32_t max_heavy) {
+                   LearnedModel *models, uint32_t leaves, uint32_t max_heavy, float bound) {
     __shared__ unsigned long long sc[kCandMax];
     __shared__ float ls[kMaxLeaves][5];           // n, sum x, sum y, sum dx*dy, sum dx*dx
     __shared__ float lmin[kMaxLeaves], lmax[kMaxLeaves];
     __shared__ uint32_t warp_tot[32];
     __shared__ double rootsum[4];
-    __shared__ uint32_t n_heavy_s, light_total_s;
+    __shared__ uint32_t n_heavy_s, light_total_s, log2_eff_s, compact_s;
     const uint32_t w = blockIdx.x;
     const SampleWin s = wins[w];
     LearnedModel &M = models[w];
@@ -186,6 +214,17 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             h++;
         }
         n_heavy_s = h;
+        // fan-out for the light keys only: about as many light tuples per
+        // bucket as the window's plan has tuples per bucket
+        uint32_t lg = s.log2_buckets;
+        while (lg > 0 && ((uint64_t)s.m << (lg - 1)) >= (light << s.log2_buckets)) lg--;
+        // the largest light key must stay well inside the overflow bound
+        const uint64_t c1 = h < nc ? (sc[h] >> 32) : (uint64_t)scr[w].cut;
+        while (lg > 0 && 2.0 * (double)c1 * (double)(1ull << lg) > (double)bound * (double)light) lg--;
+        log2_eff_s = lg;
+        // when at most half of the sample is light, the counting pass also
+        // writes the light tuples out compacted, and only those are re-read
+        compact_s = (h > 0 && 2 * light <= s.m) ? 1u : 0u;
     }
     SJBG_BARRIER();
     const uint32_t nh = n_heavy_s;
@@ -349,7 +388,8 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             prev = hi;
         }
         M.kmin = kmin; M.inv_range = inv; M.root_a = root_a; M.root_b = root_b;
-        M.leaves = leaves; M.log2_buckets = s.log2_buckets; M.fallback = total == 0 ? 1u : 0u; M.n_heavy = nh;
+        M.leaves = leaves; M.log2_buckets = log2_eff_s; M.fallback = (total == 0 && nh == 0) ? 1u : 0u; M.n_heavy = nh;
+        M.compact = compact_s;
     }
 }
 
@@ -358,16 +398,18 @@ __global__ void __launch_bounds__(kSampleThreads)
 learned_check_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *wins, const LearnedModel *models,
                      uint32_t *pred) {
     __shared__ HeavySet hs;
+    __shared__ LearnedCore core;
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
     const LearnedModel *m = &models[w];
+    if (m->fallback) return;   // whole CTA
     heavy_set_load(hs, m);
-    if (m->fallback) return;
+    copy_to_smem(&core, m, sizeof(LearnedCore));
     uint32_t *pw = pred + (uint64_t)w * kPredStride;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.m; i += gridDim.x * blockDim.x) {
         const uint32_t k = sample_key(s, L, R, i);
         if (heavy_find(hs, k) != kHeavyBucket) continue;
-        atomicAdd(&pw[learned_bucket(*m, k)], 1u);
+        atomicAdd(&pw[learned_bucket(core, k)], 1u);
     }
 }
 
@@ -380,7 +422,7 @@ learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint3
     if (M.fallback) return;
     if (threadIdx.x == 0) { mx_s = 0; sum_s = 0; }
     SJBG_BARRIER();
-    const uint32_t P = 1u << wins[w].log2_buckets;
+    const uint32_t P = 1u << M.log2_buckets;
     const uint32_t *pw = pred + (uint64_t)w * kPredStride;
     uint32_t mx = 0, sm = 0;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) { mx = max(mx, pw[i]); sm += pw[i]; }
@@ -449,9 +491,12 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     if (!hst || !dsmall || !dHist || !dTab || !dCand || !dM) return fail(h, SJBG_E_NOMEM, "learned partitioner buffers");
     uint32_t *dPred = dHist + (size_t)kBins * n;
     std::memcpy(hst, sw.data(), swB);
-    std::vector<SampleScratch> scr(n, SampleScratch{0xFFFFFFFFu, 0u, 0u, 0u});
+    SampleScratch init;
+    std::memset(&init, 0, sizeof(init));
+    init.kmin = 0xFFFFFFFFu;
+    std::vector<SampleScratch> scr(n, init);
     std::memcpy(hst + swB, scr.data(), scB);
-    SJBG_CK(h, cudaMemcpyAsync(dsmall, hst, swB + scB, cudaMemcpyHostToDevice, h->stream));
+    if (int rc_up = stage_copy(h, dsmall, hst, swB + scB)) return rc_up;
     SJBG_CK(h, cudaMemsetAsync(dHist, 0, histB + predB, h->stream));
     SJBG_CK(h, cudaMemsetAsync(dTab, 0, tabB, h->stream));
     const SampleWin *dSw = reinterpret_cast<const SampleWin *>(dsmall);
@@ -463,10 +508,12 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     SJBG_CK(h, launch(h, "learned_count", sample_count_kernel, g, dim3(kSampleThreads), 0, dL, dR, dSw,
                       (const SampleScratch *)dScr, dHist, dTab));
     const uint32_t tx = std::max<uint32_t>(1, std::min<uint32_t>(64, (uint32_t)((table_total / n + 4095) / 4096)));
+    SJBG_CK(h, launch(h, "learned_classes", heavy_classes_kernel, dim3(tx, n), dim3(kSampleThreads), 0, dSw,
+                      (const unsigned long long *)dTab, dScr));
     SJBG_CK(h, launch(h, "learned_heavy", heavy_candidates_kernel, dim3(tx, n), dim3(kSampleThreads), 0, dSw,
                       (const unsigned long long *)dTab, dScr, dCand));
     SJBG_CK(h, launch(h, "learned_fit", learned_fit_kernel, dim3(n), dim3(1024), 0, dSw, dScr, dHist, dCand, dM, leaves,
-                      allow_heavy ? kMaxHeavy : 0u));
+                      allow_heavy ? kMaxHeavy : 0u, bound));
     SJBG_CK(h, launch(h, "learned_check", learned_check_kernel, g, dim3(kSampleThreads), 0, dL, dR, dSw,
                       (const LearnedModel *)dM, dPred));
     SJBG_CK(h, launch(h, "learned_overflow", learned_overflow_kernel, dim3(n), dim3(1024), 0, dSw, dM,

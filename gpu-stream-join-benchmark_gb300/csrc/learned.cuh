@@ -13,37 +13,52 @@
 // aggregated while partitioning and combined as |L_k|*|R_k| at the end.
 #pragma once
 
+#include <cstddef>
+
 #include "common.cuh"
 
 namespace sjbg {
 
 constexpr uint32_t kMaxLeaves = 256;
 constexpr uint32_t kMaxHeavy = 512;
-constexpr uint32_t kHeavySlots = 1024;         // shared-memory heavy-key table
-constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu; // classify(): heavy key marker
+constexpr uint32_t kHeavySlotsLog2 = 11;
+constexpr uint32_t kHeavySlots = 1u << kHeavySlotsLog2;   // shared-memory heavy-key table (load <= 1/4)
+constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu;            // classify(): heavy key marker
+constexpr unsigned long long kHeavyEmpty = ~0ull;
 
-// Shared-memory heavy-key set: slot -> (key, index); empty slots hold kEmptyKey
-// in the key and 0xFFFFFFFF in the index (the index distinguishes a heavy key
-// equal to 0xFFFFFFFF from an empty slot).
-struct HeavySet {
-    uint32_t keys[kHeavySlots];
-    uint32_t idx[kHeavySlots];
+// Shared-memory heavy-key set: slot = key << 32 | index, all ones when empty
+// (a heavy index is < kMaxHeavy, so no entry is all ones).  One 64-bit load
+// per probe.
+struct __align__(16) HeavySet {   // 16-byte aligned: copied with 128-bit loads and stores
+    unsigned long long slot[kHeavySlots];
 };
 
-struct LearnedModel {
+// What classification reads: copied into shared memory (128-bit loads and
+// stores, hence the alignment) by the CTAs that classify.
+struct __align__(16) LearnedCore {
     float kmin, inv_range, root_a, root_b;
     uint32_t leaves, log2_buckets, fallback, n_heavy;
+    uint32_t compact;     // light tuples are compacted while counting (most tuples are heavy)
+    uint32_t pad_[3];
     float slope[kMaxLeaves], mean_x[kMaxLeaves], mean_y[kMaxLeaves], lo[kMaxLeaves], hi[kMaxLeaves];
+};
+
+struct LearnedModel : LearnedCore {
     uint32_t heavy_keys[kMaxHeavy];
     HeavySet heavy_set;   // built once by the fit, copied into shared memory by each CTA
 };
+
+static_assert(sizeof(LearnedCore) % 16 == 0, "LearnedCore is copied in 16-byte units");
+static_assert(sizeof(HeavySet) % 16 == 0, "HeavySet is copied in 16-byte units");
+static_assert(sizeof(LearnedModel) % 16 == 0, "models are stored back to back");
+static_assert(offsetof(LearnedModel, heavy_set) % 16 == 0, "the heavy set is copied in 16-byte units");
 
 // Per-window, per-heavy-key aggregates.
 struct HeavyAcc {
     unsigned long long cnt_l, sum_l, cnt_r, sum_r;
 };
 
-__device__ __forceinline__ uint32_t learned_bucket(const LearnedModel &m, uint32_t key) {
+__device__ __forceinline__ uint32_t learned_bucket(const LearnedCore &m, uint32_t key) {
     const uint32_t P = 1u << m.log2_buckets;
     float x = ((float)key - m.kmin) * m.inv_range;
     x = fminf(fmaxf(x, 0.0f), 1.0f);
@@ -55,45 +70,44 @@ __device__ __forceinline__ uint32_t learned_bucket(const LearnedModel &m, uint32
     return b < P ? b : P - 1;
 }
 
-__device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, 10); }
+__device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, kHeavySlotsLog2); }
 
 // Build a heavy-key set from keys[0..n) (one CTA; ends with a barrier).
 __device__ __forceinline__ void heavy_set_build(HeavySet &hs, const uint32_t *keys, uint32_t n) {
-    for (uint32_t i = threadIdx.x; i < kHeavySlots; i += blockDim.x) {
-        hs.keys[i] = kEmptyKey;
-        hs.idx[i] = 0xFFFFFFFFu;
-    }
+    for (uint32_t i = threadIdx.x; i < kHeavySlots; i += blockDim.x) hs.slot[i] = kHeavyEmpty;
     SJBG_BARRIER();
     for (uint32_t h = threadIdx.x; h < n; h += blockDim.x) {
         const uint32_t key = keys[h];
+        const unsigned long long e = ((unsigned long long)key << 32) | h;
         uint32_t s = heavy_slot(key);
         for (uint32_t p = 0; p < kHeavySlots; p++) {
-            // claim by index, which is unique per heavy key
-            if (atomicCAS(&hs.idx[s], 0xFFFFFFFFu, h) == 0xFFFFFFFFu) {
-                hs.keys[s] = key;
-                break;
-            }
+            if (atomicCAS(&hs.slot[s], kHeavyEmpty, e) == kHeavyEmpty) break;
             s = (s + 1) & (kHeavySlots - 1);
         }
     }
     SJBG_BARRIER();
 }
 
+// Copy `bytes` (a multiple of 16) from global to shared memory (all threads; ends with a barrier).
+__device__ __forceinline__ void copy_to_smem(void *dst, const void *src, uint32_t bytes) {
+    const uint4 *s = reinterpret_cast<const uint4 *>(src);
+    uint4 *d = reinterpret_cast<uint4 *>(dst);
+    for (uint32_t i = threadIdx.x; i < bytes / 16; i += blockDim.x) d[i] = s[i];
+    SJBG_BARRIER();
+}
+
 // Copy a model's prebuilt heavy-key set into shared memory (all threads; ends with a barrier).
 __device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel *m) {
-    const uint4 *src = reinterpret_cast<const uint4 *>(&m->heavy_set);
-    uint4 *dst = reinterpret_cast<uint4 *>(&hs);
-    for (uint32_t i = threadIdx.x; i < sizeof(HeavySet) / 16; i += blockDim.x) dst[i] = src[i];
-    SJBG_BARRIER();
+    copy_to_smem(&hs, &m->heavy_set, sizeof(HeavySet));
 }
 
 // Index of `key` among the heavy keys, or kHeavyBucket when it is light.
 __device__ __forceinline__ uint32_t heavy_find(const HeavySet &hs, uint32_t key) {
     uint32_t s = heavy_slot(key);
     for (uint32_t p = 0; p < kHeavySlots; p++) {
-        uint32_t id = hs.idx[s];
-        if (id == 0xFFFFFFFFu) return kHeavyBucket;
-        if (hs.keys[s] == key) return id;
+        const unsigned long long v = hs.slot[s];
+        if (v == kHeavyEmpty) return kHeavyBucket;
+        if ((uint32_t)(v >> 32) == key) return (uint32_t)v;
         s = (s + 1) & (kHeavySlots - 1);
     }
     return kHeavyBucket;

@@ -197,7 +197,7 @@ int nlj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
     if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "nested-loop plan");
     std::memcpy(hst, plan.data(), planB);
     std::memcpy(hst + planB, items.data(), itB);
-    SJBG_CK(h, cudaMemcpyAsync(dev, hst, planB + itB, cudaMemcpyHostToDevice, h->stream));
+    if (int rc_up = stage_copy(h, dev, hst, planB + itB)) return rc_up;
     const WinPlan *dPlan = reinterpret_cast<const WinPlan *>(dev);
     const NljItem *dItems = reinterpret_cast<const NljItem *>(dev + planB);
     const dim3 grid((uint32_t)items.size());

@@ -24,6 +24,7 @@ enum WsSlot : int {
     WS_MODEL, WS_SAMPLE, WS_HEAVY, WS_AUX0, WS_AUX1, WS_AUX2, WS_AUX3,
     WS_SORT_K0, WS_SORT_K1, WS_SORT_V0, WS_SORT_V1, WS_SORT_HIST,
     WS_GEN_TABLE,
+    WS_COMPACT, WS_COMPACT_CNT,      // light tuples compacted by the counting pass
     WS_COUNT
 };
 
@@ -44,6 +45,7 @@ struct sjbg_handle {
     size_t max_smem_optin = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // host-input copies overlapped with joins (created on first use)
     std::string err;
 
     sjbg::DevBuf ws[sjbg::WS_COUNT];
@@ -94,6 +96,10 @@ int cuda_fail(sjbg_handle *h, cudaError_t e, const char *what);
         if (_e != cudaSuccess) return ::sjbg::cuda_fail((h), _e, #call); \
     } while (0)
 
+// Copy between pinned host staging and device memory with a kernel, in
+// stream order on the handle's stream (no copy engine involved).
+int stage_copy(sjbg_handle *h, void *dst, const void *src, size_t bytes);
+
 // Device buffer of at least `bytes` in slot s (contents not preserved on growth).
 void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes);
 // Pinned host staging buffer i of at least `bytes`.
@@ -138,10 +144,12 @@ struct WinHost {
 };
 
 // Lazy batch drivers (device-resident inputs; pairs may be null).  They
-// accumulate into acc[n] (device, zeroed by the caller) and leave the stream
-// unsynchronised.
+// accumulate into acc[0..n) (device, zeroed by the caller), OR kErr* bits into
+// acc[n].info, and leave the stream unsynchronised.
 int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                   sjbg_pair *dPairs, WinAcc *acc, bool enumerate, uint32_t *part_used);
+int hj_global_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
+                    sjbg_pair *dPairs, WinAcc *acc, bool enumerate);
 int nlj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                    sjbg_pair *dPairs, WinAcc *acc, bool enumerate);
 int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
@@ -154,8 +162,12 @@ int generate_device(sjbg_handle *h, sjbg_tuple *out, uint64_t first, uint64_t n,
 // candidates on the batch itself the first time a shape is seen.
 int autotune_lazy(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                   bool enumerate);
-// One device-side lazy batch (no host synchronisation), used by the runtime and the tuner.
+// One device-side lazy batch (no host synchronisation), used by the runtime and
+// the tuner.  hAcc (pinned) receives n + 1 entries: the windows' accumulators,
+// then the call's device status word in hAcc[n].info (kErr* bits).
 int run_lazy_device(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                     sjbg_pair *dPairs, WinAcc *hAcc, uint32_t *part_used);
+// SJBG_OK, or the error a device status word reports (recorded on the handle).
+int device_status_error(sjbg_handle *h, unsigned long long bits);
 
 }  // namespace sjbg

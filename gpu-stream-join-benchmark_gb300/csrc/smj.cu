@@ -200,12 +200,12 @@ int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
     if (!hst || !dev || !k0 || !v0 || !k1 || !v1 || !F || !dCuts) return fail(h, SJBG_E_NOMEM, "sort-merge buffers");
     std::memcpy(hst, plan.segs.data(), segB);
     std::memcpy(hst + segB, mw.data(), mwB);
-    SJBG_CK(h, cudaMemcpyAsync(dev, hst, segB + mwB, cudaMemcpyHostToDevice, h->stream));
+    if (int rc_up = stage_copy(h, dev, hst, segB + mwB)) return rc_up;
     const SortSeg *dSegs = reinterpret_cast<const SortSeg *>(dev);
     const MergeWin *dMw = reinterpret_cast<const MergeWin *>(dev + segB);
 
     int rc = sort_extract(h, dL, dR, n, plan, dSegs, k0, v0);
-    if (!rc) rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1);
+    if (!rc) rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1, reinterpret_cast<uint32_t *>(&acc[n].info));
     if (!rc) rc = segmented_fr_prefix(h, plan, n, dSegs, v0, F);
     if (rc) return rc;
     if (tiles == 0) return SJBG_OK;

@@ -371,7 +371,7 @@ int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB,
 }
 
 int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
-                        uint32_t *keys2, uint32_t *vals2) {
+                        uint32_t *keys2, uint32_t *vals2, uint32_t *status) {
     const uint32_t nseg = (uint32_t)plan.segs.size();
     uint32_t *dMax = static_cast<uint32_t *>(ws_get(h, WS_STATUS, 64));
     uint32_t *counts = static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * plan.tiles));
@@ -399,7 +399,7 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
         SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs));
         SJBG_CK(h, launch(h, "rs_downsweep", rs_downsweep_kernel, dim3(plan.tiles), dim3(kSortThreads), smem,
                           (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, nseg, shift,
-                          (const uint32_t *)counts, dMax + 4));
+                          (const uint32_t *)counts, status));
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

@@ -49,8 +49,9 @@ __device__ __forceinline__ uint32_t find_seg(const SortSeg *segs, uint32_t nseg,
 // Stable LSD sort of every segment by key; keys/vals hold the input and the
 // sorted result on return (keys2/vals2 are scratch).  Passes = ceil(bits/8)
 // where bits covers the largest key (read back once).
+// status: a device word that receives kErrTimeout if a tile's bulk copy never lands.
 int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
-                        uint32_t *keys2, uint32_t *vals2);
+                        uint32_t *keys2, uint32_t *vals2, uint32_t *status);
 
 // Exclusive prefix sums of fr(val) (u64, mod 2^64) of the first nseg
 // segments into out (same padded layout; positions 0..n of each segment).

@@ -103,6 +103,8 @@ static void harvest(sjbg_handle *h, StreamState &st, bool wait) {
             float lat = 0.f, busy = 0.f;
             cudaEventElapsedTime(&lat, w->ev_close, w->ev_done);
             const WinAcc &a = *static_cast<const WinAcc *>(w->pinned[3].p);
+            const unsigned long long bits = static_cast<const WinAcc *>(w->pinned[3].p)[1].info;
+            if (bits) r.status = bits & kErrTimeout ? SJBG_E_TIMEOUT : SJBG_E_CAPACITY;
             r.count = a.count;
             r.prod_checksum = a.prod;
             r.partitioner_used = w->part_used;
@@ -140,7 +142,7 @@ static int launch_join(sjbg_handle *h, StreamState &st, StreamWin *w, cudaStream
     SJBG_CK(h, cudaStreamWaitEvent(h->stream, w->ev_close, 0));
     for (int i = 0; i < 6; i++) std::swap(h->pinned[i], w->pinned[i]);
     WinHost wh{0, w->n[0], 0, w->n[1], 0, 0};
-    WinAcc *hacc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc)));
+    WinAcc *hacc = static_cast<WinAcc *>(pinned_get(h, 3, 2 * sizeof(WinAcc)));   // window + status
     int rc = hacc ? run_lazy_device(h, w->buf[0] ? w->buf[0] : nullptr, w->buf[1] ? w->buf[1] : nullptr, &wh, 1,
                                     nullptr, hacc, &w->part_used)
                   : fail(h, SJBG_E_NOMEM, "window staging");

@@ -83,7 +83,7 @@ int autotune_lazy(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         h->tune = it->second;
         return SJBG_OK;
     }
-    WinAcc *hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * n));
+    WinAcc *hAcc = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc) * (n + 1)));
     if (!hAcc) return fail(h, SJBG_E_NOMEM, "tuner staging");
     cudaEvent_t e0 = event_get(h), e1 = event_get(h);
     sjbg_handle::Tune best;

@@ -70,9 +70,12 @@ def test_golden_batched_uneven_windows(lib, golden):
         assert (r["count"], r["xor"], r["prod"]) == (win["count"], win["xor"], win["prod"])
 
 
-@pytest.mark.parametrize("part", ["radix", "learned"])
+PARTS = {"radix": "PART_RADIX", "learned": "PART_LEARNED", "hbm_table": "PART_NONE"}
+
+
+@pytest.mark.parametrize("part", ["radix", "learned", "hbm_table"])
 def test_edge_cases(lib, oracle, part):
-    p = lib.PART_RADIX if part == "radix" else lib.PART_LEARNED
+    p = getattr(lib, PARTS[part])
     cases = [
         ([], []), ([1, 2, 3], []), ([], [4]), ([5], [5]),
         ([7] * 3000, [7] * 2000),                                  # one hot key
@@ -169,3 +172,82 @@ def test_profile_counts_kernels(lib, oracle):
         assert {"part_hist", "part_scan", "part_scatter", "bucket_join_count"} <= set(st)
         assert all(v[0] >= 1 and v[1] > 0 for v in st.values())
         assert j.launch_count() >= 4
+
+
+@pytest.mark.parametrize("z", [0.8, 1.0])
+def test_learned_keeps_its_model_when_many_keys_are_hot(lib, oracle, z):
+    """Zipf over a wide domain has thousands of frequently sampled keys: the
+    heaviest must still become heavy keys, so the model does not fall back,
+    and the result equals radix partitioning and the oracle."""
+    D, W = 1 << 26, 1 << 22
+    table = oracle.zipf_table(D, z)
+    left = oracle.gen_zipf(0, W, 1, table, D, 3)
+    right = oracle.gen_zipf(0, W, 2, table, D, 3)
+    want = oracle.join(left, right, enumerate_pairs=False)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=W) as j:
+        got = j.lazy_execute(left, right)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, max_tuples_per_window=W) as j:
+        rad = j.lazy_execute(left, right)
+    assert got["partitioner_used"] == lib.PART_LEARNED and not (got["flags"] & lib.WR_FALLBACK)
+    assert (got["count"], got["prod"]) == (want["count"], want["prod"]) == (rad["count"], rad["prod"])
+
+
+def test_learned_compacts_light_tuples_of_heavy_windows(lib, oracle):
+    """At z = 1.5 most tuples carry a heavy key: the counting pass compacts the
+    light ones and only those are partitioned; several windows of different
+    sizes in one call, each equal to the oracle."""
+    D = 1 << 24
+    table = oracle.zipf_table(D, 1.5)
+    sizes = [1 << 20, 3 << 18, 1 << 16, 5000]
+    lefts, rights, descs, off = [], [], [], 0
+    for n in sizes:
+        lefts.append(oracle.gen_zipf(off, n, 1, table, D, 3))
+        rights.append(oracle.gen_zipf(off, n, 2, table, D, 3))
+        descs.append((off, n, off, n, 0, 0))
+        off += n
+    left, right = np.concatenate(lefts), np.concatenate(rights)
+    want, _ = oracle.join_windows(left, right, descs, enumerate_pairs=False)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=1 << 20) as j:
+        got = j.lazy_execute_batch(left, right, descs)
+    for g, w in zip(got, want):
+        assert (g["count"], g["prod"]) == (w["count"], w["prod"])
+    assert got[0]["partitioner_used"] == lib.PART_LEARNED
+
+
+@pytest.mark.parametrize("enum", [False, True])
+def test_hbm_table_join_matches_oracle(lib, oracle, enum):
+    """The unpartitioned join (one open-addressing table per window in HBM):
+    uneven windows (including empty and single-tuple sides), uniform and Zipf
+    keys; counts, checksums and, when enumerating, the pairs."""
+    D = 1 << 16
+    table = oracle.zipf_table(D, 1.2)
+    sizes = [1 << 16, 70000, 1, 0, 4097]
+    lefts, rights, descs, off = [], [], [], 0
+    for i, n in enumerate(sizes):
+        m = n + 3   # right sides are 3 tuples longer; left sides use the first n
+        if i % 2:
+            lefts.append(oracle.gen_zipf(off, m, 1, table, D, 3))
+            rights.append(oracle.gen_zipf(off, m, 2, table, D, 3))
+        else:
+            lefts.append(oracle.gen_uniform(off, m, 1, D))
+            rights.append(oracle.gen_uniform(off, m, 2, D))
+        descs.append((off, n, off, m))
+        off += m
+    left, right = np.concatenate(lefts), np.concatenate(rights)
+    want = [oracle.join(left[d[0]:d[0] + d[1]], right[d[2]:d[2] + d[3]], enumerate_pairs=enum,
+                        pairs_capacity=1 << 22) for d in descs]
+    # pairs are written and compared for the windows with at most 2^22 of them
+    caps = [int(w["count"]) if w["count"] <= (1 << 22) else 0 for w in want]
+    pdescs = [d + (sum(caps[:i]), caps[i] if enum else 0) for i, d in enumerate(descs)]
+    pairs = np.zeros(max(sum(caps), 1), lib.PAIR_DTYPE) if enum else None
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_ATOMIC if enum else lib.RESULT_NO_OUTPUT,
+                    partitioner=lib.PART_NONE, flags=lib.F_XOR if enum else 0, max_tuples_per_window=1 << 17) as j:
+        got = j.lazy_execute_batch(left, right, pdescs, pairs=pairs)
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert (g["count"], g["prod"]) == (w["count"], w["prod"]), i
+        assert g["partitioner_used"] == lib.PART_NONE
+        if enum:
+            assert g["xor"] == w["xor"], i
+        if enum and caps[i]:
+            got_pairs = pairs[pdescs[i][4]:pdescs[i][4] + g["n_pairs"]]
+            assert np.array_equal(sorted_pairs(got_pairs), sorted_pairs(w["pairs"])), i
