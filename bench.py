@@ -149,6 +149,20 @@ def algorithmic_bytes(kernel, nwin, W, light_frac):
     return None
 
 
+def profiled_traffic(kernel, tuples):
+    """DRAM bytes of one launch from the committed ncu summary of that kernel
+    (profiles/<kernel>_*.md, line `traffic_bytes_per_tuple: X`; the capture is a
+    smaller case of the same kernel, and its traffic grows with the tuples)."""
+    import glob
+    import re
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{kernel}_*.md"))):
+        with open(path) as f:
+            m = re.search(r"^traffic_bytes_per_tuple:\s*([0-9.]+)", f.read(), flags=re.M)
+        if m:
+            return float(m.group(1)) * tuples
+    return None
+
+
 # ---------------------------------------------------------------------------- other workloads
 def _line(metric, value, unit, ms, args, workload, extra, higher=True):
     out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -506,6 +520,7 @@ def main():
     peak, peak_kind = load_peaks()
     alg = algorithmic_bytes(kname, nwin, W, light_frac)
     achieved = alg / (kms / klaunch * 1e-3) / 1e9 if alg else None
+    traffic = profiled_traffic(kname, 2 * total)
 
     # ---- end to end through the C ABI with pinned host inputs
     hL = torch.empty(total * 16, dtype=torch.uint8, pin_memory=True)
@@ -544,7 +559,9 @@ def main():
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": alg, "launch_ms": kms / klaunch, "traffic": None},
+                     "algorithmic_bytes_per_launch": alg, "launch_ms": kms / klaunch, "traffic": traffic,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per tuple of a committed ncu "
+                                       "capture (profiles/), scaled to this launch's tuples" if traffic else None},
         "kernel_ms_per_step": {k: v[1] / 3 for k, v in stats.items()},
         "clocks": clocks.summary(),
     }

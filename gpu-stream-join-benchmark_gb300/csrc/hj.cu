@@ -115,8 +115,9 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                  uint32_t *__restrict__ ccnt) {
     extern __shared__ uint32_t hist[];
     __shared__ HeavySet hs;
-    __shared__ uint32_t hcnt[kMaxHeavy];
-    __shared__ unsigned long long hsum[kMaxHeavy];
+    // heavy-key sums as two 32-bit words: native 32-bit shared atomics, with
+    // the low word's carry (seen in its returned old value) added to the high word
+    __shared__ uint32_t hcnt[kMaxHeavy], hsum_lo[kMaxHeavy], hsum_hi[kMaxHeavy];
     __shared__ uint32_t cwarp[2][32], cbase[2];   // light-tuple compaction, double-buffered by tile
     // this CTA covers tiles [t, t + kHistTiles) of one window side ("hist groups")
     const bool right = blockIdx.x >= hgroupL[nwin];
@@ -138,7 +139,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     const uint32_t P = 1u << wp.log2_buckets;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
     if (heavy) {
-        for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum[i] = 0; }
+        for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum_lo[i] = 0; hsum_hi[i] = 0; }
         heavy_set_load(hs, gm);   // ends with a barrier
     }
     SJBG_BARRIER();
@@ -181,17 +182,23 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
             if (hid != kHeavyBucket) {
                 const unsigned long long f = right ? sjbg_gs(val) : sjbg_fr(val);
-                if (hid < kRegHeavy) {
+                // predicated register sums for the hottest keys, no branch per key
 #pragma unroll
-                    for (int q = 0; q < kRegHeavy; q++)
-                        if (hid == (uint32_t)q) { rc[q]++; rs[q] += f; }
-                } else {
+                for (int q = 0; q < kRegHeavy; q++) {
+                    const bool sel = hid == (uint32_t)q;
+                    rc[q] += sel ? 1u : 0u;
+                    rs[q] += sel ? f : 0ull;
+                }
+                if (hid >= (uint32_t)kRegHeavy) {
                     atomicAdd(&hcnt[hid], 1u);
-                    atomicAdd(&hsum[hid], f);
+                    const uint32_t flo = (uint32_t)f;
+                    const uint32_t old = atomicAdd(&hsum_lo[hid], flo);
+                    atomicAdd(&hsum_hi[hid], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
                 }
             } else if (valid) {
-                atomicAdd(&hist[cls.bucket(key)], 1u);   // light keys: balanced buckets
-                lightmask |= 1u << k;
+                // light keys: compacted windows count them in part_hist_light
+                if (compact) lightmask |= 1u << k;
+                else atomicAdd(&hist[cls.bucket(key)], 1u);
             }
         } else {
             // plain partitioning: skewed keys hammer one bucket, so equal buckets
@@ -232,7 +239,9 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const unsigned long long sm = warp_sum_u64(rs[q]);
             if (lane_id() == 0 && c) {
                 atomicAdd(&hcnt[q], (uint32_t)c);
-                atomicAdd(&hsum[q], sm);
+                const uint32_t flo = (uint32_t)sm;
+                const uint32_t old = atomicAdd(&hsum_lo[q], flo);
+                atomicAdd(&hsum_hi[q], (uint32_t)(sm >> 32) + (old + flo < old ? 1u : 0u));
             }
         }
     }
@@ -244,14 +253,52 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         HeavyAcc *ha = hacc + (uint64_t)w * kMaxHeavy;
         for (uint32_t i = threadIdx.x; i < cls.m->n_heavy; i += blockDim.x) {
             if (!hcnt[i]) continue;
+            const unsigned long long sm = ((unsigned long long)hsum_hi[i] << 32) | hsum_lo[i];
             if (right) {
                 atomicAdd(&ha[i].cnt_r, (unsigned long long)hcnt[i]);
-                atomicAdd(&ha[i].sum_r, hsum[i]);
+                atomicAdd(&ha[i].sum_r, sm);
             } else {
                 atomicAdd(&ha[i].cnt_l, (unsigned long long)hcnt[i]);
-                atomicAdd(&ha[i].sum_l, hsum[i]);
+                atomicAdd(&ha[i].sum_l, sm);
             }
         }
+    }
+}
+
+// Bucket counts of the compacted light tuples of compacted learned windows
+// (part_hist only wrote them out).  Persistent CTAs stride over the tiles of
+// all window sides; tiles past a side's compacted count are skipped.
+__global__ void __launch_bounds__(kPartThreads)
+part_hist_light_kernel(const WinPlan *__restrict__ wins, uint32_t nwin, const uint32_t *__restrict__ tileL,
+                       const uint32_t *__restrict__ tileR, uint32_t *__restrict__ cnt, uint32_t B,
+                       const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
+                       const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt) {
+    extern __shared__ uint32_t hist[];
+    __shared__ LearnedCore core;
+    const uint32_t tilesL = tileL[nwin], tiles = tilesL + tileR[nwin];
+    for (uint32_t bt = blockIdx.x; bt < tiles; bt += gridDim.x) {
+        const bool right = bt >= tilesL;
+        const uint32_t t = right ? bt - tilesL : bt;
+        const uint32_t *tp = right ? tileR : tileL;
+        const uint32_t w = find_window(tp, nwin, t);
+        const WinPlan wp = wins[w];
+        const LearnedModel *gm = model_of(wp, models);
+        if (!gm || !gm->n_heavy || !gm->compact) continue;   // uniform per CTA
+        const uint64_t nside = ccnt[2 * w + (right ? 1 : 0)];
+        const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
+        if (start >= nside) continue;
+        const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+        SJBG_BARRIER();   // the previous tile's readers of hist and core are done
+        const Classifier cls = make_classifier(wp, gm, core);   // ends with a barrier
+        const uint32_t P = 1u << core.log2_buckets;
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
+        SJBG_BARRIER();
+        const uint64_t *src = (right ? compR : compL) + (uint64_t)tp[w] * kTile + start;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&hist[cls.bucket((uint32_t)__ldg(src + i))], 1u);
+        SJBG_BARRIER();
+        uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+            if (hist[i]) atomicAdd(&dst[i], hist[i]);
     }
 }
 
@@ -864,6 +911,14 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         if (learned)
             SJBG_CK(h, launch(h, "heavy_finish", heavy_finish_kernel, dim3(n), dim3(256), 0, (const WinPlan *)dPlan, n,
                               dModels, (const HeavyAcc *)dHeavy, acc));
+        if (dComp) {
+            allow_big_smem(part_hist_light_kernel, sizeof(uint32_t) * maxP);
+            const uint32_t lgrid = std::min<uint32_t>(tiles, 4u * (uint32_t)h->num_sms);
+            SJBG_CK(h, launch(h, "part_hist_light", part_hist_light_kernel, dim3(lgrid), dim3(kPartThreads),
+                              sizeof(uint32_t) * maxP, (const WinPlan *)dPlan, n, dTileL, dTileR, dCnt, (uint32_t)B,
+                              dModels, (const uint64_t *)dComp, (const uint64_t *)dComp + (uint64_t)kTile * tileL[n],
+                              (const uint32_t *)dCcnt));
+        }
         SJBG_CK(h, launch(h, "part_scan", part_scan_kernel, dim3(1), dim3(1024), 0, dCnt, dStart, dCur,
                           (uint32_t)B));
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;

@@ -21,8 +21,8 @@ namespace sjbg {
 
 constexpr uint32_t kMaxLeaves = 256;
 constexpr uint32_t kMaxHeavy = 512;
-constexpr uint32_t kHeavySlotsLog2 = 11;
-constexpr uint32_t kHeavySlots = 1u << kHeavySlotsLog2;   // shared-memory heavy-key table (load <= 1/4)
+constexpr uint32_t kHeavySlotsLog2 = 12;
+constexpr uint32_t kHeavySlots = 1u << kHeavySlotsLog2;   // shared-memory heavy-key table (load <= 1/8)
 constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu;            // classify(): heavy key marker
 constexpr unsigned long long kHeavyEmpty = ~0ull;
 
@@ -102,13 +102,18 @@ __device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel 
 }
 
 // Index of `key` among the heavy keys, or kHeavyBucket when it is light.
+// At load <= 1/8 the first slot decides almost always, so it is read without
+// a loop; only a collision walks on.
 __device__ __forceinline__ uint32_t heavy_find(const HeavySet &hs, uint32_t key) {
     uint32_t s = heavy_slot(key);
-    for (uint32_t p = 0; p < kHeavySlots; p++) {
-        const unsigned long long v = hs.slot[s];
+    unsigned long long v = hs.slot[s];
+    if (v == kHeavyEmpty) return kHeavyBucket;
+    if ((uint32_t)(v >> 32) == key) return (uint32_t)v;
+    for (uint32_t p = 1; p < kHeavySlots; p++) {
+        s = (s + 1) & (kHeavySlots - 1);
+        v = hs.slot[s];
         if (v == kHeavyEmpty) return kHeavyBucket;
         if ((uint32_t)(v >> 32) == key) return (uint32_t)v;
-        s = (s + 1) & (kHeavySlots - 1);
     }
     return kHeavyBucket;
 }
