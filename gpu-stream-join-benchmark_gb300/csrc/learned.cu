@@ -25,7 +25,7 @@
 
 namespace sjbg {
 
-constexpr uint32_t kBins = 1u << 16;     // histogram bins of the fit
+constexpr uint32_t kBins = 1u << 14;     // histogram bins of the fit (held in shared memory)
 constexpr uint32_t kCandMax = 2048;       // heavy candidates kept per window
 constexpr uint32_t kSampleThreads = 256;
 constexpr uint32_t kPredStride = 1u << 14;  // predicted-bucket counters per window (max buckets)
@@ -101,19 +101,28 @@ sample_count_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *w
     uint32_t *hw = hist + (uint64_t)w * kBins;
     unsigned long long *tw = table + s.table_off;
     const uint32_t mask = (1u << s.table_log2) - 1;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.m; i += gridDim.x * blockDim.x) {
-        const uint32_t k = sample_key(s, L, R, i);
-        atomicAdd(&hw[bin_of(key_x(k, kmin, inv))], 1u);
+    // warp-uniform trip count: equal sampled keys of a warp are combined first,
+    // so a hot key costs one atomic per warp instead of one per sample
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp_id()) * 32; base < s.m; base += warps * 32) {
+        const uint32_t i = base + lane_id();
+        const bool valid = i < s.m;
+        const uint32_t k = valid ? sample_key(s, L, R, i) : 0u;
+        const unsigned active = __ballot_sync(0xFFFFFFFFu, valid);
+        const unsigned grp = __match_any_sync(0xFFFFFFFFu, k) & active;
+        if (!valid || (int)lane_id() != __ffs(grp) - 1) continue;
+        const uint32_t c = __popc(grp);
+        atomicAdd(&hw[bin_of(key_x(k, kmin, inv))], c);
         uint32_t slot = slot_hash(k, s.table_log2);
         for (uint32_t p = 0; p <= mask; p++) {
             unsigned long long cur = tw[slot];
             if (cur == 0ull) {
-                unsigned long long prev = atomicCAS(&tw[slot], 0ull, ((unsigned long long)k << 32) | 1ull);
+                unsigned long long prev = atomicCAS(&tw[slot], 0ull, ((unsigned long long)k << 32) | c);
                 if (prev == 0ull) break;
                 cur = prev;
             }
             if ((uint32_t)(cur >> 32) == k) {
-                atomicAdd(&tw[slot], 1ull);
+                atomicAdd(&tw[slot], (unsigned long long)c);
                 break;
             }
             slot = (slot + 1) & mask;
@@ -170,11 +179,13 @@ heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, 
 __global__ void __launch_bounds__(1024)
 learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, unsigned long long *cand,
                    LearnedModel *models, uint32_t leaves, uint32_t max_heavy, float bound) {
+    extern __shared__ uint32_t fit_smem[];         // kBins histogram counters (dynamic)
     __shared__ unsigned long long sc[kCandMax];
-    __shared__ float ls[kMaxLeaves][5];           // n, sum x, sum y, sum dx*dy, sum dx*dx
-    __shared__ float lmin[kMaxLeaves], lmax[kMaxLeaves];
+    __shared__ float lfit[kMaxLeaves][5];          // per leaf: n, mean x, mean y, slope, largest y
+    __shared__ uint32_t lstart[kMaxLeaves + 1];     // first bin of each leaf
     __shared__ uint32_t warp_tot[32];
-    __shared__ double rootsum[4];
+    __shared__ double rootpart[32][2];
+    __shared__ float root_s[2];
     __shared__ uint32_t n_heavy_s, light_total_s, log2_eff_s, compact_s;
     const uint32_t w = blockIdx.x;
     const SampleWin s = wins[w];
@@ -228,168 +239,163 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     }
     SJBG_BARRIER();
     const uint32_t nh = n_heavy_s;
-    for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) {
-        const uint32_t key = ~(uint32_t)sc[h];
-        const uint32_t c = (uint32_t)(sc[h] >> 32);
-        M.heavy_keys[h] = key;
-        atomicSub(&hw[bin_of(key_x(key, kmin, inv))], c);   // light histogram only
-    }
+    for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) M.heavy_keys[h] = ~(uint32_t)sc[h];
     SJBG_BARRIER();
-    heavy_set_build(M.heavy_set, M.heavy_keys, nh);
+    heavy_set_build(M.heavy_set, M.heavy_keys, nh);   // ends with a barrier
 
-    // ---- light CDF at bin upper edges: in-place exclusive scan, then cdf_j = incl_j / total
-    const uint32_t per = kBins / blockDim.x;   // 64
-    const uint32_t b0 = threadIdx.x * per;
-    uint32_t loc = 0;
-    for (uint32_t i = 0; i < per; i++) loc += hw[b0 + i];
-    uint32_t tot;
-    const uint32_t ex = warp_excl_scan(loc, &tot);
-    if (lane_id() == 31) warp_tot[warp_id()] = ex + loc;
+    // ---- the window's light histogram, in shared memory from here on
+    uint32_t *hb = fit_smem;   // kBins counters, later the inclusive CDF counts
+    for (uint32_t i = threadIdx.x; i < kBins; i += blockDim.x) hb[i] = hw[i];
     SJBG_BARRIER();
-    if (warp_id() == 0) {
-        uint32_t x = warp_tot[lane_id()], tt;
-        const uint32_t e = warp_excl_scan(x, &tt);
-        warp_tot[lane_id()] = e;
-        if (lane_id() == 31) light_total_s = e + x;
+    for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x)
+        atomicSub(&hb[bin_of(key_x(M.heavy_keys[h], kmin, inv))], (uint32_t)(sc[h] >> 32));
+    SJBG_BARRIER();
+
+    // ---- inclusive scan: warp w owns bins [w * per, (w + 1) * per), 32 at a time
+    const uint32_t nwarps = blockDim.x >> 5, per = kBins / nwarps;
+    const uint32_t wid = warp_id(), lane = lane_id();
+    {
+        uint32_t carry = 0;
+        for (uint32_t b = wid * per; b < (wid + 1) * per; b += 32) {
+            const uint32_t v = hb[b + lane];
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan(v, &tot);
+            hb[b + lane] = carry + ex + v;
+            carry += tot;
+        }
+        if (lane == 0) warp_tot[wid] = carry;
     }
+    SJBG_BARRIER();
+    if (wid == 0) {
+        const uint32_t x = lane < nwarps ? warp_tot[lane] : 0u;
+        uint32_t tt;
+        const uint32_t e = warp_excl_scan(x, &tt);
+        warp_tot[lane] = e;
+        if (lane == 0) light_total_s = tt;
+    }
+    SJBG_BARRIER();
+    for (uint32_t b = wid * per; b < (wid + 1) * per; b += 32) hb[b + lane] += warp_tot[wid];
     SJBG_BARRIER();
     const uint32_t total = light_total_s;
-    uint32_t run = warp_tot[warp_id()] + ex;
-    for (uint32_t i = 0; i < per; i++) {
-        run += hw[b0 + i];
-        hw[b0 + i] = run;   // inclusive count at the bin's upper edge
-    }
-    if (threadIdx.x < kMaxLeaves) {
-        for (int q = 0; q < 5; q++) ls[threadIdx.x][q] = 0.0f;
-        lmin[threadIdx.x] = 2.0f;
-        lmax[threadIdx.x] = -1.0f;
-    }
-    if (threadIdx.x < 4) rootsum[threadIdx.x] = 0.0;
-    SJBG_BARRIER();
     const float invt = total ? 1.0f / (float)total : 0.0f;
 
-    // ---- root line y = a x + b over all bin points (x_j = (j+1)/kBins, y_j = cdf_j)
-    double sx = 0, sy = 0, sxx = 0, sxy = 0;
-    for (uint32_t i = 0; i < per; i++) {
-        const uint32_t j = b0 + i;
-        const double x = (double)(j + 1) / kBins, y = (double)hw[j] * invt;
-        sx += x; sy += y; sxx += x * x; sxy += x * y;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
-        sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
-        sxx += __shfl_xor_sync(0xFFFFFFFFu, sxx, o);
-        sxy += __shfl_xor_sync(0xFFFFFFFFu, sxy, o);
-    }
-    if (lane_id() == 0) {
-        atomicAdd(&rootsum[0], sx);
-        atomicAdd(&rootsum[1], sy);
-        atomicAdd(&rootsum[2], sxx);
-        atomicAdd(&rootsum[3], sxy);
-    }
-    SJBG_BARRIER();
-    const double nn = kBins;
-    const double den = nn * rootsum[2] - rootsum[0] * rootsum[0];
-    double ra = den != 0.0 ? (nn * rootsum[3] - rootsum[0] * rootsum[1]) / den : 1.0;
-    if (!(ra > 0.0)) ra = 1.0;   // the root must increase with the key
-    const double rb = (rootsum[1] - ra * rootsum[0]) / nn;
-    const float root_a = (float)ra, root_b = (float)rb;
-    auto leaf_of = [&](float x) {
-        int l = (int)floorf((root_a * x + root_b) * (float)leaves);
-        return min(max(l, 0), (int)leaves - 1);
-    };
-
-    // ---- leaf lines, pass 1: counts and means; pass 2: centred products
-    // a thread's bins are consecutive, so they fall into one or two leaves:
-    // sums are kept in registers per run of equal leaves and flushed on change
+    // ---- root line y = a x + b over the bin points x_j = (j + 1) / kBins, y_j = cdf_j;
+    // sum x and sum x^2 are closed forms, sum y and sum x*y are reduced per warp in double
     {
-        int cur = -1;
-        float c0 = 0.f, c1 = 0.f, c2 = 0.f, mn = 2.f, mxv = -1.f;
-        for (uint32_t i = 0; i <= per; i++) {
-            int l = -1;
-            float x = 0.f, y = 0.f;
-            if (i < per) {
-                const uint32_t j = b0 + i;
-                x = (float)(j + 1) / kBins;
-                y = (float)hw[j] * invt;
-                l = leaf_of(x);
-            }
-            if (l != cur) {
-                if (cur >= 0) {
-                    atomicAdd(&ls[cur][0], c0);
-                    atomicAdd(&ls[cur][1], c1);
-                    atomicAdd(&ls[cur][2], c2);
-                    atomicMin(reinterpret_cast<int *>(&lmin[cur]), __float_as_int(mn));  // y >= 0: int order == float order
-                    atomicMax(reinterpret_cast<int *>(&lmax[cur]), __float_as_int(mxv));
-                }
-                cur = l;
-                c0 = c1 = c2 = 0.f;
-                mn = 2.f;
-                mxv = -1.f;
-            }
-            if (l >= 0) {
-                c0 += 1.f; c1 += x; c2 += y;
-                mn = fminf(mn, y);
-                mxv = fmaxf(mxv, y);
-            }
+        float sy = 0.f, sxy = 0.f;
+        for (uint32_t j = threadIdx.x; j < kBins; j += blockDim.x) {
+            const float y = (float)hb[j] * invt;
+            sy += y;
+            sxy += y * ((float)(j + 1) / (float)kBins);
         }
-    }
-    SJBG_BARRIER();
-    {
-        int cur = -1;
-        float sxy = 0.f, sxx = 0.f, mx = 0.f, my = 0.f;
-        for (uint32_t i = 0; i <= per; i++) {
-            int l = -1;
-            float x = 0.f, y = 0.f;
-            if (i < per) {
-                const uint32_t j = b0 + i;
-                x = (float)(j + 1) / kBins;
-                y = (float)hw[j] * invt;
-                l = leaf_of(x);
-            }
-            if (l != cur) {
-                if (cur >= 0) {
-                    atomicAdd(&ls[cur][3], sxy);
-                    atomicAdd(&ls[cur][4], sxx);
-                }
-                cur = l;
-                sxy = sxx = 0.f;
-                if (l >= 0) {
-                    mx = ls[l][1] / ls[l][0];
-                    my = ls[l][2] / ls[l][0];
-                }
-            }
-            if (l >= 0) {
-                const float dx = x - mx, dy = y - my;
-                sxy += dx * dy;
-                sxx += dx * dx;
-            }
+        double dy = sy, dxy = sxy;
+        for (int o = 16; o > 0; o >>= 1) {
+            dy += __shfl_xor_sync(0xFFFFFFFFu, dy, o);
+            dxy += __shfl_xor_sync(0xFFFFFFFFu, dxy, o);
         }
+        if (lane == 0) { rootpart[wid][0] = dy; rootpart[wid][1] = dxy; }
     }
     SJBG_BARRIER();
     if (threadIdx.x == 0) {
-        // monotone clamps: empty leaves inherit the previous upper bound
-        float prev = 0.0f;
-        for (uint32_t l = 0; l < leaves; l++) {
-            const float n = ls[l][0];
+        double sy = 0.0, sxy = 0.0;
+        for (uint32_t q = 0; q < nwarps; q++) { sy += rootpart[q][0]; sxy += rootpart[q][1]; }
+        const double nn = kBins;
+        const double sx = (nn + 1.0) / 2.0, sxx = (nn + 1.0) * (2.0 * nn + 1.0) / (6.0 * nn);
+        const double den = nn * sxx - sx * sx;
+        double ra = den != 0.0 ? (nn * sxy - sx * sy) / den : 1.0;
+        if (!(ra > 0.0)) ra = 1.0;   // the root must increase with the key
+        root_s[0] = (float)ra;
+        root_s[1] = (float)((sy - ra * sx) / nn);
+    }
+    for (uint32_t l = threadIdx.x; l <= leaves; l += blockDim.x) lstart[l] = kBins;
+    SJBG_BARRIER();
+    const float root_a = root_s[0], root_b = root_s[1];
+    auto leaf_of = [&](uint32_t j) {
+        const float x = (float)(j + 1) / (float)kBins;
+        int l = (int)floorf((root_a * x + root_b) * (float)leaves);
+        return min(max(l, 0), (int)leaves - 1);
+    };
+    // leaf_of is non-decreasing in j, so every leaf owns a contiguous run of bins:
+    // the first bin of leaf l is where leaf_of first reaches l
+    for (uint32_t j = threadIdx.x; j < kBins; j += blockDim.x) {
+        const int lj = leaf_of(j);
+        const int lp = j ? leaf_of(j - 1) : -1;
+        for (int l = lp + 1; l <= lj; l++) lstart[l] = j;
+    }
+    SJBG_BARRIER();
+
+    // ---- one warp per leaf: centred least-squares line over the leaf's bins
+    for (uint32_t l = wid; l < leaves; l += nwarps) {
+        const uint32_t j0 = lstart[l], j1 = lstart[l + 1];
+        float c = 0.f, sx = 0.f, sy = 0.f, mxv = -1.f;
+        for (uint32_t j = j0 + lane; j < j1; j += 32) {
+            const float y = (float)hb[j] * invt;
+            c += 1.f;
+            sx += (float)(j + 1) / (float)kBins;
+            sy += y;
+            mxv = fmaxf(mxv, y);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+            sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
+            sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
+            mxv = fmaxf(mxv, __shfl_xor_sync(0xFFFFFFFFu, mxv, o));
+        }
+        const float mx = c > 0.f ? sx / c : 0.f, my = c > 0.f ? sy / c : 0.f;
+        float sxy = 0.f, sxx = 0.f;
+        for (uint32_t j = j0 + lane; j < j1; j += 32) {
+            const float dx = (float)(j + 1) / (float)kBins - mx, dy = (float)hb[j] * invt - my;
+            sxy += dx * dy;
+            sxx += dx * dx;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            sxy += __shfl_xor_sync(0xFFFFFFFFu, sxy, o);
+            sxx += __shfl_xor_sync(0xFFFFFFFFu, sxx, o);
+        }
+        if (lane == 0) {
+            float slope = sxx > 0.f ? sxy / sxx : 0.f;
+            if (!(slope >= 0.f)) slope = 0.f;
+            lfit[l][0] = c;
+            lfit[l][1] = mx;
+            lfit[l][2] = my;
+            lfit[l][3] = slope;
+            lfit[l][4] = c > 0.f ? mxv : -1.f;   // largest CDF value routed to the leaf
+        }
+    }
+    SJBG_BARRIER();
+    // ---- monotone clamps: a leaf owns the CDF range from the largest value of
+    // the leaves before it to its own largest value (prefix maximum over leaves);
+    // empty leaves inherit the previous upper bound
+    if (wid == 0) {
+        const uint32_t chunk = (leaves + 31) / 32;
+        const uint32_t l0 = lane * chunk, l1 = min(leaves, l0 + chunk);
+        float m = 0.f;
+        for (uint32_t l = l0; l < l1; l++) m = fmaxf(m, lfit[l][4]);
+        float incl = m;
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl = fmaxf(incl, y);
+        }
+        float prev = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
+        if (lane == 0) prev = 0.f;
+        for (uint32_t l = l0; l < l1; l++) {
             float lo, hi, slope, mx, my;
-            if (n < 1.0f) {
-                lo = hi = prev; slope = 0.0f; mx = 0.0f; my = prev;
+            if (lfit[l][0] < 1.f) {
+                lo = hi = prev; slope = 0.f; mx = 0.f; my = prev;
             } else {
-                mx = ls[l][1] / n; my = ls[l][2] / n;
-                slope = ls[l][4] > 0.0f ? ls[l][3] / ls[l][4] : 0.0f;
-                if (!(slope >= 0.0f)) slope = 0.0f;
-                // the leaf owns the CDF range from the previous leaf's top to its own
-                // largest sampled value: contiguous, non-overlapping, increasing ranges
+                mx = lfit[l][1]; my = lfit[l][2]; slope = lfit[l][3];
                 lo = prev;
-                hi = fmaxf(lmax[l], lo);
+                hi = fmaxf(lfit[l][4], lo);
             }
             M.slope[l] = slope; M.mean_x[l] = mx; M.mean_y[l] = my; M.lo[l] = lo; M.hi[l] = hi;
             prev = hi;
         }
-        M.kmin = kmin; M.inv_range = inv; M.root_a = root_a; M.root_b = root_b;
-        M.leaves = leaves; M.log2_buckets = log2_eff_s; M.fallback = (total == 0 && nh == 0) ? 1u : 0u; M.n_heavy = nh;
-        M.compact = compact_s;
+        if (lane == 0) {
+            M.kmin = kmin; M.inv_range = inv; M.root_a = root_a; M.root_b = root_b;
+            M.leaves = leaves; M.log2_buckets = log2_eff_s; M.fallback = (total == 0 && nh == 0) ? 1u : 0u;
+            M.n_heavy = nh;
+            M.compact = compact_s;
+        }
     }
 }
 
@@ -512,8 +518,9 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
                       (const unsigned long long *)dTab, dScr));
     SJBG_CK(h, launch(h, "learned_heavy", heavy_candidates_kernel, dim3(tx, n), dim3(kSampleThreads), 0, dSw,
                       (const unsigned long long *)dTab, dScr, dCand));
-    SJBG_CK(h, launch(h, "learned_fit", learned_fit_kernel, dim3(n), dim3(1024), 0, dSw, dScr, dHist, dCand, dM, leaves,
-                      allow_heavy ? kMaxHeavy : 0u, bound));
+    allow_big_smem(learned_fit_kernel, sizeof(uint32_t) * kBins);
+    SJBG_CK(h, launch(h, "learned_fit", learned_fit_kernel, dim3(n), dim3(1024), sizeof(uint32_t) * kBins, dSw, dScr,
+                      dHist, dCand, dM, leaves, allow_heavy ? kMaxHeavy : 0u, bound));
     SJBG_CK(h, launch(h, "learned_check", learned_check_kernel, g, dim3(kSampleThreads), 0, dL, dR, dSw,
                       (const LearnedModel *)dM, dPred));
     SJBG_CK(h, launch(h, "learned_overflow", learned_overflow_kernel, dim3(n), dim3(1024), 0, dSw, dM,
