@@ -21,8 +21,9 @@
 //        binary search into the other side's sorted run, then merged into
 //        its own run (each element's output rank = own index + rank in the
 //        other input), and the prefix sums are recomputed.
-// All kernels take scalar arguments, so sjbg_eager_run can capture a whole
-// recorded stream in one CUDA graph and replay it.
+// These per-batch kernels serve sjbg_eager_execute (the reference's
+// per-batch interface); sjbg_eager_run, which has the whole recorded stream,
+// computes the same results in a few launches (eager_run.cu).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -575,9 +576,8 @@ int sjbg_eager_run(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *rig
     int rc = eager_check(h);
     if (rc) return rc;
     if (n_batches && (!left || !right)) return fail(h, SJBG_E_INVALID, "null stream");
-    const uint64_t B = h->cfg.batch_size, W = h->cfg.window_size;
-    EagerState &st = *h->eager;
-    // host streams are copied to the device once, so the per-batch work is device to device
+    const uint64_t B = h->cfg.batch_size;
+    // host streams are copied to the device once
     const sjbg_tuple *dl = left, *dr = right;
     if (mem == SJBG_MEM_HOST && n_batches) {
         sjbg_tuple *sl = static_cast<sjbg_tuple *>(ws_get(h, WS_IN_LEFT, sizeof(sjbg_tuple) * B * n_batches));
@@ -589,40 +589,20 @@ int sjbg_eager_run(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *rig
         dr = sr;
     }
     unsigned long long *dCounts = static_cast<unsigned long long *>(ws_get(h, WS_AUX0, 8 * std::max<uint64_t>(2 * n_batches, 1)));
-    WinAcc *dWin = static_cast<WinAcc *>(ws_get(h, WS_AUX1, sizeof(WinAcc) * (2 * n_batches + 2)));
+    WinAcc *dWin = static_cast<WinAcc *>(ws_get(h, WS_AUX1, sizeof(WinAcc) * (2 * n_batches + 3)));
     if (!dCounts || !dWin) return fail(h, SJBG_E_NOMEM, "eager run buffers");
-    SJBG_CK(h, cudaMemsetAsync(dCounts, 0, 8 * std::max<uint64_t>(2 * n_batches, 1), h->stream));
     rc = eager_clear(h);
     if (rc) return rc;
-    // the reference's order (Source.cpp:20-28) and close rule (eager/CountBased.cuh:38-46)
-    uint64_t tot[2] = {0, 0};
     uint32_t windows = 0;
-    for (uint64_t b = 0; b < n_batches; b++) {
-        for (int side = 0; side < 2; side++) {
-            if (tot[0] >= W || tot[1] >= W) {
-                SJBG_CK(h, cudaMemcpyAsync(dWin + windows, st.acc, sizeof(WinAcc), cudaMemcpyDeviceToDevice, h->stream));
-                windows++;
-                rc = eager_clear(h);
-                if (rc) return rc;
-                tot[0] = tot[1] = 0;
-            }
-            const sjbg_tuple *bt = (side == 0 ? dl : dr) + b * B;
-            rc = eager_enqueue(h, bt, B, side, false, dCounts + 2 * b + side);
-            if (rc) return rc;
-            tot[side] += B;
-        }
-    }
-    if (n_batches) {
-        SJBG_CK(h, cudaMemcpyAsync(dWin + windows, st.acc, sizeof(WinAcc), cudaMemcpyDeviceToDevice, h->stream));
-        windows++;
-    }
-    std::vector<WinAcc> hw(windows);
+    rc = eager_run_batched(h, dl, dr, n_batches, eager_enumerates(h), dCounts, dWin, &windows);
+    if (rc) return rc;
+    std::vector<WinAcc> hw(windows + 1);
     if (batch_counts && n_batches)
         SJBG_CK(h, cudaMemcpyAsync(batch_counts, dCounts, 8 * 2 * n_batches, cudaMemcpyDeviceToHost, h->stream));
-    if (windows)
-        SJBG_CK(h, cudaMemcpyAsync(hw.data(), dWin, sizeof(WinAcc) * windows, cudaMemcpyDeviceToHost, h->stream));
+    SJBG_CK(h, cudaMemcpyAsync(hw.data(), dWin, sizeof(WinAcc) * (windows + 1), cudaMemcpyDeviceToHost, h->stream));
     SJBG_CK(h, cudaStreamSynchronize(h->stream));
     profile_collect(h);
+    if (int se = device_status_error(h, hw[windows].info)) return se;
     for (uint32_t w = 0; w < windows && w < n_windows_out; w++) fill_eager_result(h, hw[w], &out[w]);
     for (uint32_t w = windows; w < n_windows_out; w++) {
         std::memset(&out[w], 0, sizeof(out[w]));

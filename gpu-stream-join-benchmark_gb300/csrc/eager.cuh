@@ -35,6 +35,25 @@ struct EagerState {
     ~EagerState();
 };
 
+// One CTA of a recorded eager stream's nested-loop join (nlj.cu): left batch
+// lb against right batch rb of window `win`, left tuples [l0, l0 + tile).
+struct ERunItem {
+    uint32_t win;    // window accumulator
+    uint32_t lb;     // left batch
+    uint32_t rb;     // right batch
+    uint32_t dest;   // counter of the later batch: 2 * batch + side
+    uint32_t l0;     // first left tuple of this CTA inside the batch
+    uint32_t pad[3];
+};
+int eager_nlj_blocks(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr, uint64_t B, const ERunItem *items,
+                     uint32_t n_items, WinAcc *acc, unsigned long long *counts, bool enumerate);
+uint32_t nlj_left_tile();   // left tuples per nested-loop CTA
+
+// A whole recorded eager stream (eager_run.cu): batch counts into dCounts
+// (2 * n_batches), window totals into dWin (then the status word).
+int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr, uint64_t n_batches, bool enumerate,
+                      unsigned long long *dCounts, WinAcc *dWin, uint32_t *n_windows);
+
 int eager_init(sjbg_handle *h);
 int eager_init_and_clear(sjbg_handle *h);
 

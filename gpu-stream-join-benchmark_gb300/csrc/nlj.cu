@@ -20,7 +20,7 @@
 #include <cstring>
 #include <vector>
 
-#include "runtime.h"
+#include "eager.cuh"
 
 namespace sjbg {
 
@@ -170,6 +170,41 @@ int nlj_pair_launch(sjbg_handle *h, const sjbg_tuple *L, uint64_t nL, const sjbg
     else
         SJBG_CK(h, launch(h, "eager_nlj_count", nlj_pair_kernel<false, false>, grid, dim3(kNljThreads), 0, L,
                           (uint32_t)nL, R, (uint32_t)nR, rsplit, acc, batch_count, pairs, pairs_cap));
+    return SJBG_OK;
+}
+
+// Recorded eager streams (eager_run.cu): one CTA per (window, left batch,
+// right batch, left tile); the block pair's matches go to the later batch's
+// counter and its checksums to the window.
+uint32_t nlj_left_tile() { return kLTile; }
+
+template <bool kEnum>
+__global__ void __launch_bounds__(kNljThreads)
+eager_nlj_blocks_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, uint32_t B,
+                        const ERunItem *__restrict__ items, WinAcc *__restrict__ acc,
+                        unsigned long long *__restrict__ counts) {
+    const ERunItem it = items[blockIdx.x];
+    nlj_block<kEnum, false>(L + (uint64_t)it.lb * B, B, R + (uint64_t)it.rb * B, B, it.l0, 0, &acc[it.win],
+                            &counts[it.dest], nullptr, 0, B);
+}
+
+int eager_nlj_blocks(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr, uint64_t B, const ERunItem *items,
+                     uint32_t n_items, WinAcc *acc, unsigned long long *counts, bool enumerate) {
+    if (n_items == 0) return SJBG_OK;
+    if (B >= 0xFFFFFFFFull) return fail(h, SJBG_E_CAPACITY, "eager batches are limited to 2^32 tuples");
+    const size_t itB = sizeof(ERunItem) * n_items;
+    uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 2, itB));
+    uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_EAGER_META, itB));
+    if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "eager run plan");
+    std::memcpy(hst, items, itB);
+    if (int rc = stage_copy(h, dev, hst, itB)) return rc;
+    const ERunItem *dItems = reinterpret_cast<const ERunItem *>(dev);
+    if (enumerate)
+        SJBG_CK(h, launch(h, "erun_nlj_xor", eager_nlj_blocks_kernel<true>, dim3(n_items), dim3(kNljThreads), 0, dl,
+                          dr, (uint32_t)B, dItems, acc, counts));
+    else
+        SJBG_CK(h, launch(h, "erun_nlj_count", eager_nlj_blocks_kernel<false>, dim3(n_items), dim3(kNljThreads), 0,
+                          dl, dr, (uint32_t)B, dItems, acc, counts));
     return SJBG_OK;
 }
 

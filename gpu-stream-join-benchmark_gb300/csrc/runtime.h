@@ -25,6 +25,7 @@ enum WsSlot : int {
     WS_SORT_K0, WS_SORT_K1, WS_SORT_V0, WS_SORT_V1, WS_SORT_HIST,
     WS_GEN_TABLE,
     WS_COMPACT, WS_COMPACT_CNT,      // light tuples compacted by the counting pass
+    WS_EAGER_META, WS_EAGER_K0, WS_EAGER_K1, WS_EAGER_V0, WS_EAGER_V1, WS_EAGER_TILES,   // recorded eager streams
     WS_COUNT
 };
 
