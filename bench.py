@@ -453,8 +453,9 @@ def main():
     learned = sjbg.Joiner(partitioner=sjbg.PART_LEARNED, **flags_common)
     plain = sjbg.Joiner(partitioner=sjbg.PART_RADIX, radix_bits=plain_bits, **flags_common)
     radix_auto = sjbg.Joiner(partitioner=sjbg.PART_RADIX, **flags_common)
+    hbm_table = sjbg.Joiner(partitioner=sjbg.PART_NONE, **flags_common)
     stream = torch.cuda.Stream()
-    for j in (learned, plain, radix_auto):
+    for j in (learned, plain, radix_auto, hbm_table):
         j.set_stream(stream.cuda_stream)
 
     def run_steps(j, k, res):
@@ -485,8 +486,9 @@ def main():
     launches = (learned.launch_count() - launches0) * args.steps // (args.steps + args.warmup)
     ms_plain, res_plain = timed(plain, args.steps)
     ms_radix_auto, res_radix_auto = timed(radix_auto, args.steps)
+    ms_hbm, res_hbm = timed(hbm_table, args.steps)
     same = ([(a[0], a[1]) for a in res_learned] == [(b[0], b[1]) for b in res_plain]
-            == [(b[0], b[1]) for b in res_radix_auto])
+            == [(b[0], b[1]) for b in res_radix_auto] == [(b[0], b[1]) for b in res_hbm])
 
     # ---- per-window latency (single-window calls, device time per call)
     lat = []
@@ -550,9 +552,11 @@ def main():
         "plain": {"value": tuples / (ms_plain * 1e-3), "ms_per_step": ms_plain,
                   "partitioner": f"radix 2^{plain_bits}" if plain_bits else "radix, auto fan-out"},
         "radix_same_fanout_as_learned": {"value": tuples / (ms_radix_auto * 1e-3), "ms_per_step": ms_radix_auto},
+        "hbm_table": {"value": tuples / (ms_hbm * 1e-3), "ms_per_step": ms_hbm,
+                      "partitioner": "none: one open-addressing table per window in HBM"},
         "learned_over_plain": ms_plain / ms_learned,
         "learned_windows": sum(1 for a in res_learned if a[2] == sjbg.PART_LEARNED),
-        "outputs_identical_learned_vs_plain": same,
+        "outputs_identical_learned_vs_plain": same,   # and vs radix (learned fan-out) and the HBM table
         "latency": {"p50_ms": p50, "p99_ms": p99, "windows": len(lat), "unit": "ms per window call"},
         "e2e": {"value": tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": 32 * total,
                 "d2h_bytes_per_step": 32 * nwin, "outputs_identical": e2e_same},
@@ -574,6 +578,7 @@ def main():
     learned.close()
     plain.close()
     radix_auto.close()
+    hbm_table.close()
 
 
 if __name__ == "__main__":

@@ -1,5 +1,6 @@
 // api.cu - the extern "C" boundary (include/sjbg.h) and the handle runtime.
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -515,6 +516,12 @@ int sjbg_create(const sjbg_config *cfg, sjbg_handle **out) {
     std::unique_ptr<sjbg_handle> h(new sjbg_handle());
     h->cfg = *cfg;
     if (h->cfg.partitioner == SJBG_PART_AUTO) h->cfg.partitioner = SJBG_PART_RADIX;
+    // tuning knobs pinned from the environment (the autotuner then leaves them)
+    if (const char *e = std::getenv("SJBG_BUCKET_TARGET")) {
+        const long v = std::strtol(e, nullptr, 10);
+        if (v >= 256 && v <= (1 << 16)) h->tune.bucket_target = (uint32_t)v;
+    }
+    if (const char *e = std::getenv("SJBG_PERSISTENT_JOIN")) h->tune.persistent_join = std::atoi(e) != 0;
     h->device = cfg->device;
     if ((e = cudaSetDevice(h->device)) != cudaSuccess) return fail(nullptr, SJBG_E_CUDA, cudaGetErrorString(e));
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);

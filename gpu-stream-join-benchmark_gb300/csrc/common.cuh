@@ -47,7 +47,7 @@ struct WinPlan {
     uint32_t bucket_base;   // first global bucket id of this window
     uint32_t log2_buckets;  // buckets of this window = 1 << log2_buckets
     uint32_t model;         // learned partitioner model slot, or 0xFFFFFFFF for radix
-    uint32_t pad;
+    uint32_t two_level;     // hash join: partitioned in two passes (coarse runs, then fine buckets)
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }

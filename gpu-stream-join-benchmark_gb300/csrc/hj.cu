@@ -39,6 +39,18 @@ constexpr uint32_t kHistTiles = 16;  // tiles per histogram CTA (amortises its s
 constexpr int kPartThreads = 512;
 constexpr int kJoinThreads = 512;
 constexpr uint32_t kMaxBucketsLog2 = 14;
+// Two-level partitioning: a window of 2^lg buckets is split into 2^ceil(lg/2)
+// coarse partitions of 2^floor(lg/2) fine buckets each (at most 128 of each).
+constexpr uint32_t kCoarseMax = 128;
+constexpr uint32_t kRow = kCoarseMax + 1;   // per tile: exclusive coarse offsets, then its total
+constexpr uint32_t kGroupTiles = 64;        // tiles whose runs of one coarse partition a fine CTA gathers
+constexpr uint32_t kFineChunk = 2048;       // tuples a fine CTA sorts at a time
+constexpr int kFineThreads = 256;
+
+__host__ __device__ __forceinline__ uint32_t coarse_bits(uint32_t lg) { return (lg + 1) / 2; }
+// Windows of at least this many buckets are partitioned in two passes: with
+// fewer, a 4,096-tuple tile still writes runs of several tuples per bucket.
+constexpr uint32_t kTwoLevelMinLog2 = 11;
 
 __device__ __forceinline__ uint32_t find_window(const uint32_t *prefix, uint32_t n, uint32_t t) {
     // largest w with prefix[w] <= t  (prefix has n+1 entries, prefix[0] = 0)
@@ -112,8 +124,8 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                  const uint32_t *__restrict__ hgroupL, const uint32_t *__restrict__ hgroupR,
                  uint32_t *__restrict__ cnt, uint32_t B, const LearnedModel *__restrict__ models,
                  HeavyAcc *__restrict__ hacc, uint64_t *__restrict__ compL, uint64_t *__restrict__ compR,
-                 uint32_t *__restrict__ ccnt) {
-    extern __shared__ uint32_t hist[];
+                 uint32_t *__restrict__ ccnt, uint32_t *__restrict__ rows) {
+    extern __shared__ __align__(16) uint32_t hist[];   // P counters, then (coarse output) the tile stage
     __shared__ HeavySet hs;
     // heavy-key sums as two 32-bit words: native 32-bit shared atomics, with
     // the low word's carry (seen in its returned old value) added to the high word
@@ -133,6 +145,17 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     const bool compact = heavy && cls.m->compact;
     // compact arrays: window w's side starts at its first tile * kTile
     uint64_t *cdst = compact ? (right ? compR : compL) + (uint64_t)tp[w] * kTile : nullptr;
+    // coarse output (every window that is not compacted, when rows is given):
+    // each tile's light tuples, sorted by coarse partition, go to the same
+    // tile-sized region of the output; the tile's row holds the coarse offsets
+    const bool coarse = rows != nullptr && !compact && wp.two_level;
+    const uint32_t lgC = coarse_bits(wp.log2_buckets), cshift = wp.log2_buckets - lgC, ncoarse = 1u << lgC;
+    __shared__ uint32_t ccnt_s[kCoarseMax], cpre_s[kCoarseMax + 1];
+    uint64_t *stage = reinterpret_cast<uint64_t *>(hist + ((1u << wp.log2_buckets) + 1) / 2 * 2);
+    uint64_t *coarse_out = coarse ? (right ? compR : compL) + (uint64_t)tp[w] * kTile : nullptr;
+    uint32_t *rows_side = coarse ? rows + (right ? tileL[nwin] : 0) * kRow : nullptr;
+    if (coarse)
+        for (uint32_t i = threadIdx.x; i < ncoarse; i += blockDim.x) ccnt_s[i] = 0;
     const uint64_t nside = right ? wp.n_right : wp.n_left;
     const uint32_t t_first = (g - hp[w]) * kHistTiles;            // tile index inside the window
     const uint32_t t_end = min(t_first + kHistTiles, tp[w + 1] - tp[w]);
@@ -173,11 +196,13 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     for (int k = 0; k < kPer; k++) v[k] = nv[k];
     if (tt + 1 < t_end) load_tile(tt + 1, nv);
     uint32_t lightmask = 0;
+    uint32_t pk[kPer];   // coarse output: coarse << 16 | rank inside the tile's coarse run, or ~0u
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
         const uint32_t i = threadIdx.x + k * kPartThreads;
         const bool valid = i < n;
         const uint32_t key = v[k].x, val = v[k].y;
+        pk[k] = 0xFFFFFFFFu;
         if (heavy) {
             const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
             if (hid != kHeavyBucket) {
@@ -197,8 +222,13 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                 }
             } else if (valid) {
                 // light keys: compacted windows count them in part_hist_light
-                if (compact) lightmask |= 1u << k;
-                else atomicAdd(&hist[cls.bucket(key)], 1u);
+                if (compact) {
+                    lightmask |= 1u << k;
+                } else {
+                    const uint32_t b = cls.bucket(key);
+                    atomicAdd(&hist[b], 1u);
+                    if (coarse) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
+                }
             }
         } else {
             // plain partitioning: skewed keys hammer one bucket, so equal buckets
@@ -207,7 +237,47 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             unsigned long long gsum;
             const uint32_t b = valid ? cls.bucket(key) : 0u;
             if (warp_group(valid, b, 0ull, false, &gs, &gsum)) atomicAdd(&hist[b], gs);
+            if (coarse && valid) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
         }
+    }
+    if (coarse) {
+        SJBG_BARRIER();   // every rank of the tile is assigned
+        uint32_t *row = rows_side + (uint64_t)(tp[w] + tt) * kRow;
+        if (warp_id() == 0) {
+            // exclusive offsets of the (at most 128) coarse runs; counters reset for the next tile
+            uint32_t a[kCoarseMax / 32], sum = 0;
+#pragma unroll
+            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                const uint32_t c = lane_id() * (kCoarseMax / 32) + q;
+                a[q] = c < ncoarse ? ccnt_s[c] : 0u;
+                sum += a[q];
+            }
+            uint32_t tot;
+            uint32_t run = warp_excl_scan(sum, &tot);
+#pragma unroll
+            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                const uint32_t c = lane_id() * (kCoarseMax / 32) + q;
+                if (c < ncoarse) {
+                    cpre_s[c] = run;
+                    row[c] = run;
+                    ccnt_s[c] = 0;
+                }
+                run += a[q];
+            }
+            if (lane_id() == 0) {
+                cpre_s[ncoarse] = tot;
+                row[ncoarse] = tot;
+            }
+        }
+        SJBG_BARRIER();
+#pragma unroll
+        for (int k = 0; k < kPer; k++)
+            if (pk[k] != 0xFFFFFFFFu) stage[cpre_s[pk[k] >> 16] + (pk[k] & 0xFFFFu)] = ((uint64_t)v[k].y << 32) | v[k].x;
+        SJBG_BARRIER();
+        // the tile's light tuples, contiguous per coarse run, written out whole
+        const uint32_t nl = cpre_s[ncoarse];
+        uint64_t *dst = coarse_out + (uint64_t)tt * kTile;
+        for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) dst[i] = stage[i];
     }
     if (compact) {
         // the tile's light tuples go to the window side's compact array as
@@ -398,23 +468,26 @@ __device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
 }
 
 // ------------------------------------------------------------------ 3. scatter
-__global__ void __launch_bounds__(kPartThreads, 3)
-part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
-                    uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
-                    uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
-                    const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
-                    const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt) {
+__device__ __forceinline__ void scatter_tile(uint32_t bt, const sjbg_tuple *__restrict__ L,
+                                             const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
+                                             uint32_t nwin, const uint32_t *__restrict__ tileL,
+                                             const uint32_t *__restrict__ tileR, uint32_t *__restrict__ cursor,
+                                             uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
+                                             const LearnedModel *__restrict__ models,
+                                             const uint64_t *__restrict__ compL, const uint64_t *__restrict__ compR,
+                                             const uint32_t *__restrict__ ccnt, bool skip_two_level) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t warp_tot[32];
     const uint32_t tilesL = tileL[nwin];
-    const bool right = blockIdx.x >= tilesL;
-    const uint32_t t = right ? blockIdx.x - tilesL : blockIdx.x;
+    const bool right = bt >= tilesL;
+    const uint32_t t = right ? bt - tilesL : bt;
     const uint32_t *tp = right ? tileR : tileL;
     const uint32_t w = find_window(tp, nwin, t);
     const WinPlan wp = wins[w];
     const LearnedModel *gm = model_of(wp, models);
     // compacted windows: the tiles cover the light tuples the counting pass wrote out
     const bool compact = gm && gm->n_heavy && gm->compact;
+    if (skip_two_level && !compact && wp.two_level) return;   // whole CTA: part_fine partitions this window
     const uint64_t nside = compact ? ccnt[2 * w + (right ? 1 : 0)] : (right ? wp.n_right : wp.n_left);
     const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
     if (start >= nside) return;   // whole CTA
@@ -492,27 +565,209 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
     }
 }
 
+__global__ void __launch_bounds__(kPartThreads, 3)
+part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
+                    uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                    uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
+                    const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
+                    const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt, bool skip_two_level) {
+    // persistent CTAs over the tiles of every window side (most tiles of
+    // compacted windows are past their packed light tuples and end at once)
+    const uint32_t tiles = tileL[nwin] + tileR[nwin];
+    for (uint32_t bt = blockIdx.x; bt < tiles; bt += gridDim.x) {
+        SJBG_BARRIER();   // the previous tile's shared-memory readers are done
+        scatter_tile(bt, L, R, wins, nwin, tileL, tileR, cursor, B, outL, outR, models, compL, compR, ccnt,
+                     skip_two_level);
+    }
+}
+
+
+// ------------------------------------------------------------------ 3'. fine pass
+// Two-level windows: one work item per (window side, coarse partition c,
+// group of kGroupTiles tiles) gathers the tiles' runs of partition c (about
+// kTile / 2^lgC tuples each, contiguous) with asynchronous 8-byte copies into
+// shared memory, and scatters them into the partition's 2^(lg - lgC) fine
+// buckets: a local counting sort of up to kFineChunk tuples, one global
+// reservation per fine bucket, then contiguous per-bucket runs - coalesced
+// writes however many buckets the window has.  Persistent CTAs take the items
+// in turn; items of other windows end at once.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+constexpr size_t kFineSmem = kFineChunk * (2 * sizeof(uint64_t) + sizeof(uint8_t));
+
+__device__ __forceinline__ void fine_item(uint32_t bi, const WinPlan *__restrict__ wins, uint32_t nwin,
+                                          const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                                          const uint32_t *__restrict__ itemL, const uint32_t *__restrict__ itemR,
+                                          uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL,
+                                          uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
+                                          const uint64_t *__restrict__ srcL, const uint64_t *__restrict__ srcR,
+                                          const uint32_t *__restrict__ rows) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    uint64_t *tmp = reinterpret_cast<uint64_t *>(smem_raw);       // kFineChunk gathered tuples
+    uint64_t *stage = tmp + kFineChunk;                            // kFineChunk, sorted by fine bucket
+    uint8_t *sf = reinterpret_cast<uint8_t *>(stage + kFineChunk); // kFineChunk fine ids
+    __shared__ uint32_t runoff[kGroupTiles], runpre[kGroupTiles + 1];
+    __shared__ uint32_t fcnt[kCoarseMax], floc[kCoarseMax], fbase[kCoarseMax];
+    __shared__ LearnedCore core;
+    const bool right = bi >= itemL[nwin];
+    const uint32_t item = right ? bi - itemL[nwin] : bi;
+    const uint32_t *ip = right ? itemR : itemL;
+    const uint32_t *tp = right ? tileR : tileL;
+    const uint32_t w = find_window(ip, nwin, item);
+    const WinPlan wp = wins[w];
+    if (!wp.two_level) return;   // whole CTA
+    const LearnedModel *gm = model_of(wp, models);
+    if (gm && gm->n_heavy && gm->compact) return;   // compacted windows: part_scatter
+    const uint32_t lg = wp.log2_buckets, lgC = coarse_bits(lg), cshift = lg - lgC, nfine = 1u << cshift;
+    const uint32_t ntw = tp[w + 1] - tp[w];
+    const uint32_t ngroups = (ntw + kGroupTiles - 1) / kGroupTiles;
+    const uint32_t local = item - ip[w];
+    const uint32_t c = local / ngroups, g = local % ngroups;
+    const uint32_t t0 = g * kGroupTiles, G = min(kGroupTiles, ntw - t0);
+    const Classifier cls = make_classifier(wp, gm, core);   // ends with a barrier when there is a model
+    const uint32_t *rows_side = rows + (right ? tileL[nwin] : 0) * kRow;
+    if (warp_id() == 0) {
+        // the runs of partition c in tiles t0 .. t0 + G, and their prefix
+        uint32_t len[2], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const uint32_t i = lane_id() * 2 + q;
+            len[q] = 0;
+            if (i < G) {
+                const uint32_t *row = rows_side + (uint64_t)(tp[w] + t0 + i) * kRow;
+                const uint32_t off = row[c];
+                len[q] = row[c + 1] - off;
+                runoff[i] = (t0 + i) * kTile + off;
+            }
+            sum += len[q];
+        }
+        uint32_t tot;
+        uint32_t run = warp_excl_scan(sum, &tot);
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const uint32_t i = lane_id() * 2 + q;
+            if (i < G) runpre[i] = run;
+            run += len[q];
+        }
+        if (lane_id() == 0) runpre[G] = tot;
+    }
+    SJBG_BARRIER();
+    const uint32_t T = runpre[G];
+    const uint64_t *src = (right ? srcR : srcL) + (uint64_t)tp[w] * kTile;
+    uint64_t *out = right ? outR : outL;
+    uint32_t *gcur = cursor + (right ? B : 0) + wp.bucket_base + (c << cshift);
+    constexpr int kPer = kFineChunk / kFineThreads;
+    const uint32_t nwarps = blockDim.x >> 5;
+    for (uint32_t ch = 0; ch < T; ch += kFineChunk) {
+        const uint32_t m = min(kFineChunk, T - ch);
+        for (uint32_t f = threadIdx.x; f < nfine; f += blockDim.x) fcnt[f] = 0;
+        // gather: warp r % nwarps copies the part of run r inside [ch, ch + m)
+        for (uint32_t r = warp_id(); r < G; r += nwarps) {
+            const uint32_t a = max(runpre[r], ch), b = min(runpre[r + 1], ch + m);
+            for (uint32_t x = a + lane_id(); x < b; x += 32)
+                cp_async8(tmp + (x - ch), src + runoff[r] + (x - runpre[r]));
+        }
+        cp_async_wait_all();
+        SJBG_BARRIER();
+        uint64_t e[kPer];
+        uint32_t fr[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const uint32_t j = threadIdx.x + k * kFineThreads;
+            fr[k] = 0xFFFFFFFFu;
+            if (j < m) {
+                e[k] = tmp[j];
+                const uint32_t f = cls.bucket((uint32_t)e[k]) & (nfine - 1);
+                fr[k] = (f << 16) | atomicAdd(&fcnt[f], 1u);
+            }
+        }
+        SJBG_BARRIER();
+        if (warp_id() == 0) {
+            uint32_t a[kCoarseMax / 32], sum = 0;
+#pragma unroll
+            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                const uint32_t f = lane_id() * (kCoarseMax / 32) + q;
+                a[q] = f < nfine ? fcnt[f] : 0u;
+                sum += a[q];
+            }
+            uint32_t tot;
+            uint32_t run = warp_excl_scan(sum, &tot);
+#pragma unroll
+            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                const uint32_t f = lane_id() * (kCoarseMax / 32) + q;
+                if (f < nfine) {
+                    floc[f] = run;
+                    fbase[f] = a[q] ? atomicAdd(&gcur[f], a[q]) : 0u;
+                }
+                run += a[q];
+            }
+        }
+        SJBG_BARRIER();
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            if (fr[k] != 0xFFFFFFFFu) {
+                const uint32_t pos = floc[fr[k] >> 16] + (fr[k] & 0xFFFFu);
+                stage[pos] = e[k];
+                sf[pos] = (uint8_t)(fr[k] >> 16);
+            }
+        }
+        SJBG_BARRIER();
+        for (uint32_t pos = threadIdx.x; pos < m; pos += blockDim.x) {
+            const uint32_t f = sf[pos];
+            out[fbase[f] + (pos - floc[f])] = stage[pos];
+        }
+        SJBG_BARRIER();
+    }
+}
+
+__global__ void __launch_bounds__(kFineThreads, 4)
+part_fine_kernel(const WinPlan *__restrict__ wins, uint32_t nwin, const uint32_t *__restrict__ tileL,
+                 const uint32_t *__restrict__ tileR, const uint32_t *__restrict__ itemL,
+                 const uint32_t *__restrict__ itemR, uint32_t *__restrict__ cursor, uint32_t B,
+                 uint64_t *__restrict__ outL, uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
+                 const uint64_t *__restrict__ srcL, const uint64_t *__restrict__ srcR,
+                 const uint32_t *__restrict__ rows) {
+    const uint32_t items = itemL[nwin] + itemR[nwin];
+    for (uint32_t bi = blockIdx.x; bi < items; bi += gridDim.x) {
+        SJBG_BARRIER();   // the previous item's shared-memory readers are done
+        fine_item(bi, wins, nwin, tileL, tileR, itemL, itemR, cursor, B, outL, outR, models, srcL, srcR, rows);
+    }
+}
+
 // ------------------------------------------------------------------ 4. bucket join
 constexpr uint32_t kMaxProbe = 64;   // linear-probe bound of the count tables
+
+// Count-table slots for buckets of about `target` left tuples (load <= 0.77).
+static inline uint32_t count_table_cap(uint32_t target) { return (target * 13u / 10u + 31u) & ~31u; }
 
 struct CountTable {
     uint32_t *keys;              // C + 1 (slot C reserved for key 0xFFFFFFFF)
     uint32_t *cnt;               // C + 1
     unsigned long long *sumf;    // C + 1
-    uint32_t bits;
+    uint32_t C;                  // slots (any size: the hash is scaled, not masked)
 };
+
+// Home slot of a key in a table of C slots: a 32-bit multiplicative hash scaled to [0, C).
+__device__ __forceinline__ uint32_t ct_home(uint32_t key, uint32_t C) {
+    return (uint32_t)(((uint64_t)slot_hash(key, 32) * C) >> 32);
+}
 
 // Insert `c` tuples of `key` with fr-sum `f`.  A key that finds neither itself
 // nor a free slot within kMaxProbe slots is refused (false) and joined in a
 // later pass; lookups use the same bound, so a refused key is never half-found.
 __device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uint32_t c, unsigned long long f) {
-    const uint32_t C = 1u << t.bits;
+    const uint32_t C = t.C;
     if (key == kEmptyKey) {
         atomicAdd(&t.cnt[C], c);
         atomicAdd(&t.sumf[C], f);
         return true;
     }
-    uint32_t s = slot_hash(key, t.bits);
+    uint32_t s = ct_home(key, C);
     for (uint32_t probe = 0; probe < kMaxProbe; probe++) {
         uint32_t k = *(volatile uint32_t *)&t.keys[s];
         if (k == kEmptyKey) {
@@ -524,20 +779,20 @@ __device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uin
             atomicAdd(&t.sumf[s], f);
             return true;
         }
-        s = (s + 1) & (C - 1);
+        s = s + 1 == C ? 0 : s + 1;
     }
     return false;
 }
 
 __device__ __forceinline__ int ct_lookup(const CountTable &t, uint32_t key) {
-    const uint32_t C = 1u << t.bits;
+    const uint32_t C = t.C;
     if (key == kEmptyKey) return t.cnt[C] ? (int)C : -1;
-    uint32_t s = slot_hash(key, t.bits);
+    uint32_t s = ct_home(key, C);
     for (uint32_t probe = 0; probe < kMaxProbe; probe++) {
         const uint32_t k = t.keys[s];
         if (k == key) return (int)s;
         if (k == kEmptyKey) return -1;
-        s = (s + 1) & (C - 1);
+        s = s + 1 == C ? 0 : s + 1;
     }
     return -1;
 }
@@ -573,23 +828,22 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
                                                   const uint64_t *__restrict__ partR,
                                                   const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt,
                                                   uint32_t B, const uint32_t *__restrict__ bucket_win,
-                                                  WinAcc *__restrict__ acc, uint32_t table_bits) {
+                                                  WinAcc *__restrict__ acc, uint32_t cap) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t novf;
     const uint32_t nR = cnt[b], nS = cnt[B + b];
     if (nR == 0 || nS == 0) return;
     uint64_t *Rb = partL + start[b];
     const uint64_t *Sb = partR + start[B + b];
-    // the table holds at most nR distinct keys: twice that many slots (at
-    // least 64, at most the launch's table) keep small buckets cheap to clear
-    uint32_t bits = 6;
-    while (bits < table_bits && (1u << bits) < 2 * nR) bits++;
-    const uint32_t C = 1u << bits;
+    // the table holds at most nR distinct keys: 1.3x that many slots (load
+    // <= 0.77; at least 64, at most the launch's capacity) keep small buckets
+    // cheap to clear and let two CTAs share an SM
+    const uint32_t C = min(cap, max(64u, (nR * 13u / 10u + 31u) & ~31u));
     CountTable t;
     t.sumf = reinterpret_cast<unsigned long long *>(smem_raw);
     t.keys = reinterpret_cast<uint32_t *>(t.sumf + C + 1);
     t.cnt = t.keys + C + 1;
-    t.bits = bits;
+    t.C = C;
     const uint32_t tile = kJoinPer * blockDim.x;
 
     unsigned long long count = 0, prod = 0;
@@ -763,10 +1017,10 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
 __global__ void __launch_bounds__(kJoinThreads)
 bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
-                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t table_bits,
+                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t cap,
                          uint32_t *queue) {
     if (!queue) {
-        join_count_bucket(blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc, table_bits);
+        join_count_bucket(blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc, cap);
         return;
     }
     __shared__ uint32_t item_s;
@@ -776,7 +1030,7 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
         SJBG_BARRIER();
         const uint32_t b = item_s;
         if (b >= B) break;
-        join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, table_bits);
+        join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, cap);
     }
 }
 
@@ -823,9 +1077,10 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     // ---- plan
     std::vector<WinPlan> plan(n);
-    std::vector<uint32_t> tileL(n + 1), tileR(n + 1), hgL(n + 1), hgR(n + 1);
+    std::vector<uint32_t> tileL(n + 1), tileR(n + 1), hgL(n + 1), hgR(n + 1), itL(n + 1), itR(n + 1);
     uint64_t B = 0, totL = 0, totR = 0;
     uint32_t maxP = 1;
+    bool any_two = false, any_one = false;
     for (uint32_t w = 0; w < n; w++) {
         const WinHost &wh = wins[w];
         WinPlan &p = plan[w];
@@ -840,12 +1095,19 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         p.log2_buckets = lg;
         p.bucket_base = (uint32_t)B;
         p.model = 0xFFFFFFFFu;
+        p.two_level = lg >= kTwoLevelMinLog2 ? 1u : 0u;
+        any_two |= p.two_level != 0;
+        any_one |= p.two_level == 0;
         B += 1ull << lg;
         maxP = std::max(maxP, 1u << lg);
         tileL[w + 1] = tileL[w] + (uint32_t)((wh.n_left + kTile - 1) / kTile);
         tileR[w + 1] = tileR[w] + (uint32_t)((wh.n_right + kTile - 1) / kTile);
         hgL[w + 1] = hgL[w] + (tileL[w + 1] - tileL[w] + kHistTiles - 1) / kHistTiles;
         hgR[w + 1] = hgR[w] + (tileR[w + 1] - tileR[w] + kHistTiles - 1) / kHistTiles;
+        // fine-pass CTAs: coarse partitions x groups of kGroupTiles tiles
+        const uint32_t nc = 1u << coarse_bits(lg);
+        itL[w + 1] = itL[w] + nc * ((tileL[w + 1] - tileL[w] + kGroupTiles - 1) / kGroupTiles);
+        itR[w + 1] = itR[w] + nc * ((tileR[w + 1] - tileR[w] + kGroupTiles - 1) / kGroupTiles);
         totL += wh.n_left;
         totR += wh.n_right;
     }
@@ -857,7 +1119,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     // ---- upload plan, tile prefixes and bucket->window map in one copy
     const size_t planB = sizeof(WinPlan) * n, tileB = sizeof(uint32_t) * (n + 1), bwB = sizeof(uint32_t) * B;
-    const size_t upB = planB + 4 * tileB + bwB;
+    const size_t upB = planB + 6 * tileB + bwB;
     uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 0, upB));
     uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_WIN_PLAN, upB));
     if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "plan buffers");
@@ -866,14 +1128,18 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     std::memcpy(hst + planB + tileB, tileR.data(), tileB);
     std::memcpy(hst + planB + 2 * tileB, hgL.data(), tileB);
     std::memcpy(hst + planB + 3 * tileB, hgR.data(), tileB);
-    std::memcpy(hst + planB + 4 * tileB, bwin.data(), bwB);
+    std::memcpy(hst + planB + 4 * tileB, itL.data(), tileB);
+    std::memcpy(hst + planB + 5 * tileB, itR.data(), tileB);
+    std::memcpy(hst + planB + 6 * tileB, bwin.data(), bwB);
     if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
     WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
     const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
     const uint32_t *dTileR = reinterpret_cast<const uint32_t *>(dev + planB + tileB);
     const uint32_t *dHgL = reinterpret_cast<const uint32_t *>(dev + planB + 2 * tileB);
     const uint32_t *dHgR = reinterpret_cast<const uint32_t *>(dev + planB + 3 * tileB);
-    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 4 * tileB);
+    const uint32_t *dItL = reinterpret_cast<const uint32_t *>(dev + planB + 4 * tileB);
+    const uint32_t *dItR = reinterpret_cast<const uint32_t *>(dev + planB + 5 * tileB);
+    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 6 * tileB);
 
     uint32_t *dCnt = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CNT, sizeof(uint32_t) * 2 * B));
     uint32_t *dStart = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_START, sizeof(uint32_t) * 2 * B));
@@ -884,49 +1150,62 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     const LearnedModel *dModels = nullptr;
     HeavyAcc *dHeavy = nullptr;
-    uint64_t *dComp = nullptr;
-    uint32_t *dCcnt = nullptr;
     if (learned) {
         int rc = learned_prepare(h, dL, dR, plan.data(), n, dPlan, &dModels, !enumerate);
         if (rc) return rc;
         dHeavy = static_cast<HeavyAcc *>(ws_get(h, WS_HEAVY, sizeof(HeavyAcc) * kMaxHeavy * n));
         if (!dHeavy) return fail(h, SJBG_E_NOMEM, "heavy-key accumulators");
         SJBG_CK(h, cudaMemsetAsync(dHeavy, 0, sizeof(HeavyAcc) * kMaxHeavy * n, h->stream));
-        if (!enumerate) {   // heavy keys exist only in count mode
-            dComp = static_cast<uint64_t *>(
-                ws_get(h, WS_COMPACT, sizeof(uint64_t) * kTile * ((uint64_t)tileL[n] + tileR[n])));
-            dCcnt = static_cast<uint32_t *>(ws_get(h, WS_COMPACT_CNT, sizeof(uint32_t) * 2 * n));
-            if (!dComp || !dCcnt) return fail(h, SJBG_E_NOMEM, "compaction buffers");
-            SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * 2 * n, h->stream));
-        }
     }
+    // the counting pass's output: per window side and tile, its light tuples
+    // (compacted windows: packed at the side's start; others: sorted by coarse
+    // partition inside the tile's own region), plus the tiles' coarse rows
+    const uint64_t tiles64 = (uint64_t)tileL[n] + tileR[n];
+    uint64_t *dComp = static_cast<uint64_t *>(ws_get(h, WS_COMPACT, sizeof(uint64_t) * kTile * std::max<uint64_t>(tiles64, 1)));
+    uint32_t *dRows = static_cast<uint32_t *>(ws_get(h, WS_COARSE_ROWS, sizeof(uint32_t) * kRow * std::max<uint64_t>(tiles64, 1)));
+    uint32_t *dCcnt = static_cast<uint32_t *>(ws_get(h, WS_COMPACT_CNT, sizeof(uint32_t) * 2 * n));
+    if (!dComp || !dRows || !dCcnt) return fail(h, SJBG_E_NOMEM, "partition staging buffers");
+    SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * 2 * n, h->stream));
+    uint64_t *dCompR = dComp + (uint64_t)kTile * tileL[n];
 
     SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
     const uint32_t tiles = tileL[n] + tileR[n];
     if (tiles) {
-        allow_big_smem(part_hist_kernel, sizeof(uint32_t) * maxP);
-        SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(hgL[n] + hgR[n]), dim3(kPartThreads),
-                          sizeof(uint32_t) * maxP, dL, dR, dPlan, n, dTileL, dTileR, dHgL, dHgR, dCnt, (uint32_t)B,
-                          dModels, dHeavy, dComp, dComp ? dComp + (uint64_t)kTile * tileL[n] : nullptr, dCcnt));
+        const size_t histSmem = sizeof(uint32_t) * ((maxP + 1) / 2 * 2) + sizeof(uint64_t) * kTile;
+        allow_big_smem(part_hist_kernel, histSmem);
+        SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(hgL[n] + hgR[n]), dim3(kPartThreads), histSmem, dL,
+                          dR, dPlan, n, dTileL, dTileR, dHgL, dHgR, dCnt, (uint32_t)B, dModels, dHeavy, dComp, dCompR,
+                          dCcnt, dRows));
         if (learned)
             SJBG_CK(h, launch(h, "heavy_finish", heavy_finish_kernel, dim3(n), dim3(256), 0, (const WinPlan *)dPlan, n,
                               dModels, (const HeavyAcc *)dHeavy, acc));
-        if (dComp) {
+        if (learned && !enumerate) {   // compacted windows exist only with heavy keys
             allow_big_smem(part_hist_light_kernel, sizeof(uint32_t) * maxP);
             const uint32_t lgrid = std::min<uint32_t>(tiles, 4u * (uint32_t)h->num_sms);
             SJBG_CK(h, launch(h, "part_hist_light", part_hist_light_kernel, dim3(lgrid), dim3(kPartThreads),
                               sizeof(uint32_t) * maxP, (const WinPlan *)dPlan, n, dTileL, dTileR, dCnt, (uint32_t)B,
-                              dModels, (const uint64_t *)dComp, (const uint64_t *)dComp + (uint64_t)kTile * tileL[n],
-                              (const uint32_t *)dCcnt));
+                              dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dCcnt));
         }
         SJBG_CK(h, launch(h, "part_scan", part_scan_kernel, dim3(1), dim3(1024), 0, dCnt, dStart, dCur,
                           (uint32_t)B));
-        const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;
-        allow_big_smem(part_scatter_kernel, scatterSmem);
-        SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(tiles), dim3(kPartThreads), scatterSmem,
-                          dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels,
-                          (const uint64_t *)dComp, dComp ? (const uint64_t *)dComp + (uint64_t)kTile * tileL[n] : nullptr,
-                          (const uint32_t *)dCcnt));
+        // single-level windows, and compacted windows (their packed light tuples):
+        // a local counting sort per tile
+        if (any_one || (learned && !enumerate)) {
+            const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;
+            allow_big_smem(part_scatter_kernel, scatterSmem);
+            const uint32_t sgrid = std::min<uint32_t>(tiles, 3u * 4u * (uint32_t)h->num_sms);
+            SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(sgrid), dim3(kPartThreads), scatterSmem,
+                              dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels,
+                              (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dCcnt, true));
+        }
+        // two-level windows: the fine pass over the tiles' coarse runs
+        if (any_two && itL[n] + itR[n]) {
+            allow_big_smem(part_fine_kernel, kFineSmem);
+            const uint32_t fgrid = std::min<uint32_t>(itL[n] + itR[n], 4u * 4u * (uint32_t)h->num_sms);
+            SJBG_CK(h, launch(h, "part_fine", part_fine_kernel, dim3(fgrid), dim3(kFineThreads), kFineSmem,
+                              (const WinPlan *)dPlan, n, dTileL, dTileR, dItL, dItR, dCur, (uint32_t)B, dPL, dPR,
+                              dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dRows));
+        }
     }
     // persistent CTAs draining a work queue of buckets, or one CTA per bucket
     uint32_t *queue = nullptr;
@@ -945,11 +1224,15 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         SJBG_CK(h, launch(h, "bucket_join_enum", bucket_join_enum_kernel, jgrid, dim3(kJoinThreads), smem,
                           dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits, queue));
     } else {
-        const uint32_t bits = 13;
-        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
+        const uint32_t cap = count_table_cap((uint32_t)target);
+        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
+        if (queue) {   // as many persistent CTAs as fit on an SM at this table size (at most 2 by registers)
+            const uint32_t per_sm = std::max<uint32_t>(1, (uint32_t)((228u << 10) / (smem + 1024)));
+            jgrid = dim3((uint32_t)std::min<uint64_t>(B, (uint64_t)h->num_sms * std::min<uint32_t>(per_sm, 2u)));
+        }
         SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, jgrid, dim3(kJoinThreads), smem,
-                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, bits, queue));
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, cap, queue));
     }
     return SJBG_OK;
 }
@@ -972,7 +1255,7 @@ __global__ void raw_setup_kernel(RawScratch *rs, uint32_t *bucket_win, uint32_t 
         WinPlan &p = rs->plan;
         p.left_off = 0; p.n_left = nL; p.right_off = 0; p.n_right = nR;
         p.pairs_off = 0; p.pairs_cap = 0;
-        p.bucket_base = 0; p.log2_buckets = lg; p.model = 0xFFFFFFFFu; p.pad = 0;
+        p.bucket_base = 0; p.log2_buckets = lg; p.model = 0xFFFFFFFFu; p.two_level = 0;
         rs->tile[0] = 0; rs->tile[1] = tL;
         rs->tile[2] = 0; rs->tile[3] = tR;
         rs->tile[4] = 0; rs->tile[5] = (tL + kHistTiles - 1) / kHistTiles;
@@ -1031,16 +1314,18 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         const uint32_t groups = (tL + kHistTiles - 1) / kHistTiles + (tR + kHistTiles - 1) / kHistTiles;
         allow_big_smem(part_hist_kernel, sizeof(uint32_t) * P);
         part_hist_kernel<<<groups, kPartThreads, sizeof(uint32_t) * P, st>>>(
-            dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr, nullptr, nullptr, nullptr);
+            dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr, nullptr, nullptr, nullptr,
+            nullptr);
         part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * P;
         allow_big_smem(part_scatter_kernel, scatterSmem);
         part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, cur, P, pL,
-                                                                          pR, nullptr, nullptr, nullptr, nullptr);
-        const uint32_t bits = 13;
-        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * ((1u << bits) + 1) + 16;
+                                                                          pR, nullptr, nullptr, nullptr, nullptr,
+                                                                          false);
+        const uint32_t cap = count_table_cap(4096);
+        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
-        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, bits, nullptr);
+        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, cap, nullptr);
     }
     raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);
     return cudaGetLastError() == cudaSuccess ? SJBG_OK : SJBG_E_CUDA;

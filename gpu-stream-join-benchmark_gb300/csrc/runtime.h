@@ -24,7 +24,8 @@ enum WsSlot : int {
     WS_MODEL, WS_SAMPLE, WS_HEAVY, WS_AUX0, WS_AUX1, WS_AUX2, WS_AUX3,
     WS_SORT_K0, WS_SORT_K1, WS_SORT_V0, WS_SORT_V1, WS_SORT_HIST,
     WS_GEN_TABLE,
-    WS_COMPACT, WS_COMPACT_CNT,      // light tuples compacted by the counting pass
+    WS_COMPACT, WS_COMPACT_CNT,      // light tuples written by the counting pass
+    WS_COARSE_ROWS,                  // per tile: coarse-partition offsets of its light tuples
     WS_EAGER_META, WS_EAGER_K0, WS_EAGER_K1, WS_EAGER_V0, WS_EAGER_V1, WS_EAGER_TILES,   // recorded eager streams
     WS_COUNT
 };

@@ -169,7 +169,8 @@ def test_profile_counts_kernels(lib, oracle):
     with lib.Joiner(lib.ALG_HJ, lib.LAZY, flags=lib.F_PROFILE, max_tuples_per_window=W) as j:
         j.lazy_execute(left, left)
         st = j.kernel_stats()
-        assert {"part_hist", "part_scan", "part_scatter", "bucket_join_count"} <= set(st)
+        assert {"part_hist", "part_scan", "bucket_join_count"} <= set(st)
+        assert "part_scatter" in st or "part_fine" in st
         assert all(v[0] >= 1 and v[1] > 0 for v in st.values())
         assert j.launch_count() >= 4
 
