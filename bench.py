@@ -144,8 +144,12 @@ def algorithmic_bytes(kernel, nwin, W, light_frac):
         return 16 * n
     if kernel == "part_scatter":
         return 16 * n + 8 * n * light_frac
+    if kernel == "part_fine":
+        return 16 * n * light_frac
     if kernel.startswith("bucket_join"):
         return 8 * n * light_frac
+    if kernel.startswith("ht_build") or kernel.startswith("ht_probe"):
+        return 16 * n // 2   # one side's tuples (the table traffic is not counted)
     return None
 
 
@@ -308,11 +312,16 @@ def bench_stream(args, sjbg, torch, dev, rate=1e9, seconds=3.0, window_ms=100, c
             if not times:
                 continue
             n = len(times) * B
+            if n > cap:
+                raise RuntimeError("a chunk of Poisson batches exceeds the staging buffer")
             z = 0.8 if times[0] < end_ns / 3 else (1.2 if times[0] < 2 * end_ns / 3 else 1.5)
             buf = bufs[side]
             j.generate(buf.data_ptr(), first[side], n, 1 + side, D, tables[z].data_ptr(), 3)
             ts = torch.tensor(times, dtype=torch.int64, device="cuda").repeat_interleave(B)
             buf[:n * 16].view(torch.int64).view(-1, 2)[:, 1] = ts
+            # the event times are written on torch's stream; the library reads the
+            # batch on its own stream, so the write must be complete first
+            torch.cuda.current_stream().synchronize()
             first[side] += n
             # pace: do not push data before its event time has come (wall clock)
             wait = times[-1] * 1e-9 - (time.perf_counter() - t0)
@@ -450,7 +459,11 @@ def main():
 
     windows = [(w * W, W, w * W, W, 0, 0) for w in range(nwin)]
     descs = (sjbg.WindowDesc * nwin)(*[sjbg.WindowDesc(*d) for d in windows])
-    learned = sjbg.Joiner(partitioner=sjbg.PART_LEARNED, **flags_common)
+    # the headline arm: learned partitioning on skewed windows; on uniform keys
+    # the library's automatic choice (one HBM table per window while the tables
+    # stay inside L2, else radix partitioning)
+    primary_part = sjbg.PART_LEARNED if z is not None else sjbg.PART_AUTO
+    learned = sjbg.Joiner(partitioner=primary_part, **flags_common)
     plain = sjbg.Joiner(partitioner=sjbg.PART_RADIX, radix_bits=plain_bits, **flags_common)
     radix_auto = sjbg.Joiner(partitioner=sjbg.PART_RADIX, **flags_common)
     hbm_table = sjbg.Joiner(partitioner=sjbg.PART_NONE, **flags_common)
@@ -505,7 +518,7 @@ def main():
     p99 = lat[min(len(lat) - 1, int(0.99 * len(lat)))]
 
     # ---- roofline of the dominant kernel (event-timed launches of a profiling pass)
-    prof = sjbg.Joiner(partitioner=sjbg.PART_LEARNED, flags=sjbg.F_PROFILE, **flags_common)
+    prof = sjbg.Joiner(partitioner=primary_part, flags=sjbg.F_PROFILE, **flags_common)
     prof.set_stream(stream.cuda_stream)
     res = (sjbg.WindowResult * nwin)()
     run_steps(prof, 1, res)
@@ -545,7 +558,9 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_learned,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": args.workload, "windows": nwin, "tuples_per_window_per_stream": W,
-                   "key_domain": D, "zipf_z": z, "partitioner": "learned (256 leaves, 1% sample)",
+                   "key_domain": D, "zipf_z": z,
+                   "partitioner": ("learned (256 leaves, 1% sample)" if z is not None
+                                   else "auto (HBM table per window in L2, else radix)"),
                    "learned_fanout": "auto (about 4096 left tuples per bucket)",
                    "l2": (f"inputs larger than L2 ({total * 32 >> 20} MiB per step)" if total * 32 > (129 << 20)
                           else "L2-resident inputs")},

@@ -212,7 +212,7 @@ static void fill_result(const sjbg_handle *h, const WinAcc &a, const WinHost &w,
 // captured with private pinned staging buffers; later identical calls replay it.
 static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                       sjbg_pair *dPairs, bool enumerate, sjbg_window_result *out) {
-    std::vector<uint64_t> key = {h->cfg.algorithm, h->cfg.partitioner, h->cfg.flags, h->cfg.result_mode,
+    std::vector<uint64_t> key = {h->cfg.algorithm, h->cfg.partitioner, h->tune.partitioner, h->cfg.flags, h->cfg.result_mode,
                                  (uint64_t)(uintptr_t)dL, (uint64_t)(uintptr_t)dR, (uint64_t)(uintptr_t)dPairs, n,
                                  h->tune.bucket_target, (uint64_t)h->tune.persistent_join,
                                  (uint64_t)(uintptr_t)h->stream};
@@ -515,7 +515,7 @@ int sjbg_create(const sjbg_config *cfg, sjbg_handle **out) {
     if (cfg->device < 0 || cfg->device >= ndev) return fail(nullptr, SJBG_E_INVALID, "bad device ordinal");
     std::unique_ptr<sjbg_handle> h(new sjbg_handle());
     h->cfg = *cfg;
-    if (h->cfg.partitioner == SJBG_PART_AUTO) h->cfg.partitioner = SJBG_PART_RADIX;
+    // SJBG_PART_AUTO stays: each hash-join call picks (hj.cu: choose_partitioner)
     // tuning knobs pinned from the environment (the autotuner then leaves them)
     if (const char *e = std::getenv("SJBG_BUCKET_TARGET")) {
         const long v = std::strtol(e, nullptr, 10);

@@ -1062,10 +1062,25 @@ static uint32_t ceil_log2(uint64_t x) {
     return b;
 }
 
+// The partitioner of a call: the configured one, or for SJBG_PART_AUTO the
+// autotuner's choice, else one HBM table per window when every window's table
+// stays well inside L2 (at most 2^18 left tuples, 2^21 over the call), else
+// radix partitioning.
+uint32_t choose_partitioner(const sjbg_handle *h, const WinHost *wins, uint32_t n) {
+    if (h->cfg.partitioner != SJBG_PART_AUTO) return h->cfg.partitioner;
+    if (h->tune.partitioner) return h->tune.partitioner;
+    uint64_t tot = 0, mx = 0;
+    for (uint32_t w = 0; w < n; w++) {
+        tot += wins[w].n_left;
+        mx = std::max(mx, wins[w].n_left);
+    }
+    return (mx <= (1u << 18) && tot <= (1u << 21)) ? SJBG_PART_NONE : SJBG_PART_RADIX;
+}
+
 int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                   sjbg_pair *dPairs, WinAcc *acc, bool enumerate, uint32_t *part_used) {
     if (n == 0) return SJBG_OK;
-    const uint32_t part = h->cfg.partitioner;
+    const uint32_t part = choose_partitioner(h, wins, n);
     if (part == SJBG_PART_NONE) {   // one HBM table per window (hj_global.cu)
         if (part_used) *part_used = SJBG_PART_NONE;
         return hj_global_batch(h, dL, dR, wins, n, dPairs, acc, enumerate);

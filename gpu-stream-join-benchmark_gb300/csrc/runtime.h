@@ -67,6 +67,7 @@ struct sjbg_handle {
     struct Tune {
         uint32_t bucket_target = 4096;   // left tuples per hash-join bucket
         bool persistent_join = true;     // bucket join drains a device work queue
+        uint32_t partitioner = 0;        // SJBG_PART_AUTO handles: the tuned choice (0 = by window size)
         float ms = 0.0f;                 // measured time of the chosen setting (autotuner)
     } tune;
 
@@ -150,6 +151,7 @@ struct WinHost {
 // acc[n].info, and leave the stream unsynchronised.
 int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                   sjbg_pair *dPairs, WinAcc *acc, bool enumerate, uint32_t *part_used);
+uint32_t choose_partitioner(const sjbg_handle *h, const WinHost *wins, uint32_t n);
 int hj_global_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,
                     sjbg_pair *dPairs, WinAcc *acc, bool enumerate);
 int nlj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinHost *wins, uint32_t n,

@@ -3,7 +3,8 @@
 // No reference counterpart.  For a batch shape (algorithm, partitioner,
 // enumeration, log2 of the tuples and of the windows) not seen before, the
 // candidate settings - left tuples per bucket (which sets the partition
-// fan-out) and persistent vs one-CTA-per-bucket joins - are each run on the
+// fan-out), persistent vs one-CTA-per-bucket joins and, for SJBG_PART_AUTO
+// handles, one HBM table per window vs radix partitioning - are each run on the
 // batch itself, timed with CUDA events, and the fastest is kept.  Decisions
 // are persisted as JSON lines in $SJBG_TUNE_CACHE (default
 // ~/.cache/sjbg_tune.json) and reloaded by later handles.
@@ -12,6 +13,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <vector>
 
 #include <sys/stat.h>
 
@@ -33,14 +35,16 @@ static void tune_load(sjbg_handle *h) {
     std::string line;
     while (std::getline(f, line)) {
         char shape[256] = {0};
-        unsigned target = 0, persistent = 0;
+        unsigned target = 0, persistent = 0, part = 0;
         float ms = 0.f;
-        if (std::sscanf(line.c_str(), " {\"shape\": \"%255[^\"]\", \"bucket_target\": %u, \"persistent\": %u, \"ms\": %f",
-                        shape, &target, &persistent, &ms) == 4 &&
-            (target == 2048 || target == 4096 || target == 8192)) {
+        if (std::sscanf(line.c_str(),
+                        " {\"shape\": \"%255[^\"]\", \"bucket_target\": %u, \"persistent\": %u, \"partitioner\": %u, \"ms\": %f",
+                        shape, &target, &persistent, &part, &ms) == 5 &&
+            (target == 2048 || target == 4096 || target == 8192) && part <= SJBG_PART_LEARNED) {
             sjbg_handle::Tune t;
             t.bucket_target = target;
             t.persistent_join = persistent != 0;
+            t.partitioner = part;
             t.ms = ms;
             h->tuned[shape] = t;
         }
@@ -59,7 +63,8 @@ static void tune_save(const sjbg_handle *h) {
     if (!f) return;   // a read-only home only loses the cache
     for (const auto &kv : h->tuned)
         f << "{\"shape\": \"" << kv.first << "\", \"bucket_target\": " << kv.second.bucket_target
-          << ", \"persistent\": " << (kv.second.persistent_join ? 1 : 0) << ", \"ms\": " << kv.second.ms << "}\n";
+          << ", \"persistent\": " << (kv.second.persistent_join ? 1 : 0) << ", \"partitioner\": "
+          << kv.second.partitioner << ", \"ms\": " << kv.second.ms << "}\n";
 }
 
 static uint32_t log2u(uint64_t x) {
@@ -88,9 +93,17 @@ int autotune_lazy(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     cudaEvent_t e0 = event_get(h), e1 = event_get(h);
     sjbg_handle::Tune best;
     best.ms = 1e30f;
+    // partitioners tried: the configured one, or for SJBG_PART_AUTO the HBM
+    // table and radix partitioning
+    std::vector<uint32_t> parts;
+    if (h->cfg.partitioner == SJBG_PART_AUTO) parts = {SJBG_PART_NONE, SJBG_PART_RADIX};
+    else parts = {0u};
+    for (uint32_t part : parts)
     for (uint32_t target : {2048u, 4096u, 8192u}) {
         for (bool persistent : {false, true}) {
             if (enumerate && persistent) continue;   // chain-building joins run one CTA per bucket
+            if (part == SJBG_PART_NONE && (target != 4096u || !persistent)) continue;   // no buckets to tune
+            h->tune.partitioner = part;
             h->tune.bucket_target = target;
             h->tune.persistent_join = persistent;
             uint32_t pu;

@@ -166,7 +166,8 @@ def test_device_generator_matches_host(lib, oracle):
 def test_profile_counts_kernels(lib, oracle):
     W = 4096
     left = oracle.gen_uniform(0, W, 1, W)
-    with lib.Joiner(lib.ALG_HJ, lib.LAZY, flags=lib.F_PROFILE, max_tuples_per_window=W) as j:
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, flags=lib.F_PROFILE,
+                    max_tuples_per_window=W) as j:
         j.lazy_execute(left, left)
         st = j.kernel_stats()
         assert {"part_hist", "part_scan", "bucket_join_count"} <= set(st)
@@ -252,3 +253,16 @@ def test_hbm_table_join_matches_oracle(lib, oracle, enum):
         if enum and caps[i]:
             got_pairs = pairs[pdescs[i][4]:pdescs[i][4] + g["n_pairs"]]
             assert np.array_equal(sorted_pairs(got_pairs), sorted_pairs(w["pairs"])), i
+
+
+def test_auto_partitioner_by_window_size(lib, oracle):
+    """SJBG_PART_AUTO: windows whose tables stay in L2 get one HBM table per
+    window, larger windows radix partitioning; both equal the oracle."""
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, max_tuples_per_window=1 << 20) as j:
+        for W, part in ((1 << 14, lib.PART_NONE), (1 << 20, lib.PART_RADIX)):
+            left = oracle.gen_uniform(0, W, 1, W)
+            right = oracle.gen_uniform(0, W, 2, W)
+            want = oracle.join(left, right, enumerate_pairs=False)
+            got = j.lazy_execute(left, right)
+            assert got["partitioner_used"] == part
+            assert (got["count"], got["prod"]) == (want["count"], want["prod"])
