@@ -159,18 +159,17 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     const uint64_t nside = right ? wp.n_right : wp.n_left;
     const uint32_t t_first = (g - hp[w]) * kHistTiles;            // tile index inside the window
     const uint32_t t_end = min(t_first + kHistTiles, tp[w + 1] - tp[w]);
-    const uint32_t P = 1u << wp.log2_buckets;
+    // counters of the buckets in use: the model's own fan-out when there is one
+    const uint32_t P = 1u << (cls.m ? cls.m->log2_buckets : wp.log2_buckets);
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
     if (heavy) {
         for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum_lo[i] = 0; hsum_hi[i] = 0; }
         heavy_set_load(hs, gm);   // ends with a barrier
     }
     SJBG_BARRIER();
-    // the hottest heavy keys (the fit orders heavy keys by sampled count) are
-    // accumulated in registers; other heavy keys with shared atomics
-    constexpr int kRegHeavy = 4;
-    uint32_t rc[kRegHeavy] = {0, 0, 0, 0};
-    unsigned long long rs[kRegHeavy] = {0, 0, 0, 0};
+    // heavy keys are summed with shared atomics only: measured, that beats
+    // keeping the hottest keys' sums in registers (fewer instructions per tuple
+    // outweigh the atomics' serialisation on the hottest keys)
     constexpr int kPer = kTile / kPartThreads;
     const sjbg_tuple *base = right ? R + wp.right_off : L + wp.left_off;
     // key and val of the thread's tuples of tile tt (the sectors read are those
@@ -207,19 +206,10 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
             if (hid != kHeavyBucket) {
                 const unsigned long long f = right ? sjbg_gs(val) : sjbg_fr(val);
-                // predicated register sums for the hottest keys, no branch per key
-#pragma unroll
-                for (int q = 0; q < kRegHeavy; q++) {
-                    const bool sel = hid == (uint32_t)q;
-                    rc[q] += sel ? 1u : 0u;
-                    rs[q] += sel ? f : 0ull;
-                }
-                if (hid >= (uint32_t)kRegHeavy) {
-                    atomicAdd(&hcnt[hid], 1u);
-                    const uint32_t flo = (uint32_t)f;
-                    const uint32_t old = atomicAdd(&hsum_lo[hid], flo);
-                    atomicAdd(&hsum_hi[hid], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
-                }
+                atomicAdd(&hcnt[hid], 1u);
+                const uint32_t flo = (uint32_t)f;
+                const uint32_t old = atomicAdd(&hsum_lo[hid], flo);
+                atomicAdd(&hsum_hi[hid], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
             } else if (valid) {
                 // light keys: compacted windows count them in part_hist_light
                 if (compact) {
@@ -301,19 +291,6 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         for (int k = 0; k < kPer; k++)
             if ((lightmask >> k) & 1u) cdst[pos++] = ((uint64_t)v[k].y << 32) | v[k].x;
     }
-    }
-    if (heavy) {
-#pragma unroll
-        for (int q = 0; q < kRegHeavy; q++) {
-            const unsigned long long c = warp_sum_u64(rc[q]);
-            const unsigned long long sm = warp_sum_u64(rs[q]);
-            if (lane_id() == 0 && c) {
-                atomicAdd(&hcnt[q], (uint32_t)c);
-                const uint32_t flo = (uint32_t)sm;
-                const uint32_t old = atomicAdd(&hsum_lo[q], flo);
-                atomicAdd(&hsum_hi[q], (uint32_t)(sm >> 32) + (old + flo < old ? 1u : 0u));
-            }
-        }
     }
     SJBG_BARRIER();
     uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
@@ -494,7 +471,8 @@ __device__ __forceinline__ void scatter_tile(uint32_t bt, const sjbg_tuple *__re
     const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
     const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
     const uint64_t *csrc = compact ? (right ? compR : compL) + (uint64_t)tp[w] * kTile + start : nullptr;
-    const uint32_t P = 1u << wp.log2_buckets;
+    // a model buckets into its own (often smaller) fan-out: only those counters are touched
+    const uint32_t P = 1u << (gm ? gm->log2_buckets : wp.log2_buckets);
 
     uint64_t *stage = reinterpret_cast<uint64_t *>(smem_raw);                  // kTile
     uint16_t *sb = reinterpret_cast<uint16_t *>(stage + kTile);                // kTile bucket ids
