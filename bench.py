@@ -65,13 +65,13 @@ class ClockSampler:
 
     def run(self):
         q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,power.draw")
         while not self.stop_flag.is_set():
             try:
                 out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={q}",
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
                 v = [x.strip() for x in out.stdout.strip().split(",")]
-                if len(v) == 6:
+                if len(v) == 7:
                     self.samples.append(v)
             except (OSError, subprocess.SubprocessError):
                 return
@@ -92,8 +92,15 @@ class ClockSampler:
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        pw = []
+        for s in self.samples:
+            try:
+                pw.append(float(s[6]))
+            except ValueError:
+                pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples),
+                "power_w_median": statistics.median(pw) if pw else None}
 
 
 # ---------------------------------------------------------------------------- reference arm

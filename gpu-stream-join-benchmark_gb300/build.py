@@ -87,7 +87,7 @@ def build_harness(force: bool = False) -> str | None:
     cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", HOST,
            "-I", os.path.join(cuda, "include")] + srcs + [
         "-o", HARNESS, "-L", LIBDIR, "-lsjbg", "-Wl,-rpath,$ORIGIN", "-L", cudalib, "-lcudart",
-        "-Wl,-rpath," + cudalib, "-lpthread"]
+        "-Wl,-rpath," + cudalib, "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"harness build failed:\n{r.stdout}\n{r.stderr}")

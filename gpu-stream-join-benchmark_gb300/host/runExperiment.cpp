@@ -123,10 +123,14 @@ std::pair<std::string, uint64_t> runExperimentWithConfig(const ExperimentConfig 
         Sink sink;
         auto windowing = Windowing::WindowingFactory::create(config.algorithmConfig, config.dataConfig,
                                                              config.queryConfig, config.engineConfig, sink);
+        PowerSampler power;   // power_data.txt, as the reference writes it
+        if (config.measurePower) power.start();
         auto t0 = std::chrono::high_resolution_clock::now();
         sink.markProcessingStart();
         source.start(left, right, config.sourceThreads, windowing);
         auto t1 = std::chrono::high_resolution_clock::now();
+        power.end();
+        if (config.measurePower) LOG_INFO("Power samples: %u (power_data.txt)", power.samples());
         msElapsed = std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count();
         const uint64_t matchCount = sink.getMatchCount();
         const double selectivity = 100.0 * matchCount / std::max<uint64_t>(1, sink.getPossibleMatches());

@@ -3,11 +3,14 @@
 #include "sjb_host.hpp"
 
 #include <algorithm>
+#include <cstdio>
 #include <cctype>
 #include <condition_variable>
 #include <fstream>
 #include <sstream>
 #include <thread>
+
+#include <dlfcn.h>
 
 namespace {
 
@@ -375,6 +378,69 @@ void Source::start(Tuple *leftTuples, Tuple *rightTuples, uint64_t sourceThreads
     for (auto &t : ts) t.join();
     if (err) std::rethrow_exception(err);
     windowing->onEndOfStream();
+}
+
+// ---- PowerSampler ----
+namespace {
+// The few NVML entry points used, resolved from libnvidia-ml at run time.
+struct Nvml {
+    void *lib = nullptr;
+    int (*init)() = nullptr;
+    int (*shutdown)() = nullptr;
+    int (*handle)(unsigned, void **) = nullptr;
+    int (*power)(void *, unsigned *) = nullptr;   // milliwatts
+    bool load() {
+        lib = dlopen("libnvidia-ml.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!lib) return false;
+        init = reinterpret_cast<int (*)()>(dlsym(lib, "nvmlInit_v2"));
+        shutdown = reinterpret_cast<int (*)()>(dlsym(lib, "nvmlShutdown"));
+        handle = reinterpret_cast<int (*)(unsigned, void **)>(dlsym(lib, "nvmlDeviceGetHandleByIndex_v2"));
+        power = reinterpret_cast<int (*)(void *, unsigned *)>(dlsym(lib, "nvmlDeviceGetPowerUsage"));
+        return init && shutdown && handle && power;
+    }
+};
+}  // namespace
+
+bool PowerSampler::start() {
+    if (thread) return true;
+    auto *nv = new Nvml();
+    void *dev = nullptr;
+    if (!nv->load() || nv->init() != 0 || nv->handle(0, &dev) != 0) {
+        std::fprintf(stderr, "runExperiment: NVML unavailable, power is not measured\n");
+        if (nv->lib) dlclose(nv->lib);
+        delete nv;
+        return false;
+    }
+    run = true;
+    n = 0;
+    thread = new std::thread([this, nv, dev] {
+        FILE *fp = std::fopen(path.c_str(), "a");
+        while (run) {
+            unsigned mw = 0;
+            if (fp && nv->power(dev, &mw) == 0) {
+                const long long ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+                                         std::chrono::system_clock::now().time_since_epoch())
+                                         .count();
+                std::fprintf(fp, "%lld,%.3f\n", ms, mw / 1000.0);
+                n++;
+            }
+            std::this_thread::sleep_for(std::chrono::milliseconds(period_ms));
+        }
+        if (fp) std::fclose(fp);
+        nv->shutdown();
+        dlclose(nv->lib);
+        delete nv;
+    });
+    return true;
+}
+
+void PowerSampler::end() {
+    if (!thread) return;
+    run = false;
+    auto *t = static_cast<std::thread *>(thread);
+    t->join();
+    delete t;
+    thread = nullptr;
 }
 
 // ---- YamlLite ----

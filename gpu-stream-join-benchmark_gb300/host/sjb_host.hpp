@@ -272,6 +272,30 @@ private:
     uint64_t count, bufferSize;
 };
 
+// GPU power sampling while an experiment runs (measurePowerUsage: "Yes"),
+// the role of the reference's PowerMeasurementAgent
+// (src/sjb/utils/PowerMeasurementAgent.cpp:50-175): a thread reads the board
+// power of GPU 0 through NVML every `period_ms` and appends "epoch_ms,watts"
+// lines to a file.  NVML is loaded at run time; when it is missing, start()
+// says so on stderr and the experiment runs unmeasured.  Read-only: no GPU
+// setting is changed.
+class PowerSampler {
+public:
+    explicit PowerSampler(std::string path = "power_data.txt", unsigned period_ms = 10)
+        : path(std::move(path)), period_ms(period_ms) {}
+    ~PowerSampler() { end(); }
+    bool start();
+    void end();
+    unsigned samples() const { return n; }
+
+private:
+    std::string path;
+    unsigned period_ms;
+    std::atomic<bool> run{false};
+    std::atomic<unsigned> n{0};
+    void *thread = nullptr;   // std::thread, kept opaque
+};
+
 // Minimal reader of the flat YAML the reference's configs use: `key: value`
 // and `key: [a, "b", c]` lines with `#` comments.
 class YamlLite {

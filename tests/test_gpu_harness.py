@@ -17,16 +17,17 @@ B = 1 << 13            # batchSizeKB: [128]
 DISTINCT = 1000
 
 
-def run(harness, tmp_path, alg, prog, result="NoOutput", theta="0.0", distinct=DISTINCT):
+def run(harness, tmp_path, alg, prog, result="NoOutput", theta="0.0", distinct=DISTINCT, power="No"):
     y = tmp_path / "exp.yaml"
     y.write_text(
         f'algTypes: [ "{alg}" ]\ndeviceTypes: [ "GPU" ]\nprogressivenessModes: [ "{prog}" ]\n'
         f"distinctKeys: [ {distinct} ]\nzipfThetas: [ {theta} ]\nresultMaterializationMethod: [ \"{result}\" ]\n"
         f'windowSizesMB: [ 1 ]\nbatchSizeKB: [ 128 ]\nmeasuredMetric: "cumulativePercentage"\n'
-        f'measurePowerUsage: "No"\nrepeat: 1\nparStrats: [ "INTRA" ]\ndataSize: {N}\nsourceThreads: 1\n')
+        f'measurePowerUsage: "{power}"\nrepeat: 1\nparStrats: [ "INTRA" ]\ndataSize: {N}\nsourceThreads: 1\n')
     r = subprocess.run([harness, str(y), str(tmp_path / "out.csv")], capture_output=True, text=True,
                        cwd=tmp_path, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
+    run.last = r
     m = re.search(r"Match Count: (\d+)", r.stdout)
     p = re.search(r"Prod checksum: (\d+)", r.stdout)
     w = re.search(r"Windows: (\d+)", r.stdout)
@@ -83,3 +84,16 @@ def test_eager_harness_matches_oracle(harness, oracle, tmp_path, alg):
     assert count == int(bc.sum())
     assert progress == np.cumsum(bc).tolist()          # one progress record per batch, arrival order
     assert windows == len(wc) - 1                      # closes counted; the last window stays open
+
+
+def test_power_samples_written(harness, tmp_path):
+    """measurePowerUsage: "Yes" samples the GPU's power while the experiment
+    runs and appends epoch-ms,watts lines to power_data.txt, as the
+    reference's power agent does."""
+    run(harness, tmp_path, "HJ", "LAZY", power="Yes")
+    if "NVML unavailable" in run.last.stderr:
+        pytest.skip("NVML is not available on this machine")
+    lines = (tmp_path / "power_data.txt").read_text().strip().splitlines()
+    assert lines
+    ms, watts = lines[0].split(",")
+    assert int(ms) > 0 and 0.0 < float(watts) < 5000.0
