@@ -6,10 +6,12 @@
 // is the lazy CPU_HJ's (src/sjb/windowing/lazy/executor/CPU/CPU_HJ.cpp:30-136):
 // every left tuple joins every right tuple of the window with an equal key.
 //
-// Design (many windows per call, four launches in total):
+// Design (many windows per call, one launch per pass):
 //   1. part_hist     per 4096-tuple tile: bucket of each tuple -> shared histogram
 //                    -> one atomicAdd per non-empty bucket into the global counts.
-//   2. part_scan     exclusive scan of the counts of both sides -> bucket starts.
+//   2. part_scan     per window, exclusive scan of its counts on both sides ->
+//                    bucket starts; buckets with tuples on both sides form the
+//                    join list, the only buckets step 4 visits.
 //   3. part_scatter  per tile: local counting sort by bucket in shared memory,
 //                    one atomicAdd per bucket to reserve a range, then the tile
 //                    is written as contiguous per-bucket runs of (key,val) words.
@@ -315,25 +317,78 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
 // Bucket counts of the compacted light tuples of compacted learned windows
 // (part_hist only wrote them out).  Persistent CTAs stride over the tiles of
 // all window sides; tiles past a side's compacted count are skipped.
+// Per window side, the tiles (or fine items) that each later pass has work
+// for, as exclusive prefixes over the windows, written once the counting pass
+// is done: kind 0 part_hist_light (the compacted windows' light tiles), kind 1
+// part_scatter (those, plus every tile of a single-level window that was not
+// compacted), kind 2 part_fine (two-level windows that were not compacted).
+// Array 2 * kind + side (left 0, right 1) of n + 1 entries.  One warp per array.
+enum : uint32_t { kWorkLight = 0, kWorkScatter = 1, kWorkFine = 2 };
+__global__ void part_work_kernel(const WinPlan *__restrict__ wins, uint32_t nwin, const uint32_t *__restrict__ tileL,
+                                 const uint32_t *__restrict__ tileR, const uint32_t *__restrict__ itemL,
+                                 const uint32_t *__restrict__ itemR, const LearnedModel *__restrict__ models,
+                                 const uint32_t *__restrict__ ccnt, uint32_t *__restrict__ work) {
+    const uint32_t a = warp_id();
+    if (a >= 6) return;   // whole warp
+    const uint32_t kind = a >> 1, right = a & 1u;
+    const uint32_t *tp = right ? tileR : tileL, *ip = right ? itemR : itemL;
+    uint32_t *out = work + a * (nwin + 1);
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nwin; base += 32) {
+        const uint32_t w = base + lane_id();
+        uint32_t c = 0;
+        if (w < nwin) {
+            const WinPlan wp = wins[w];
+            const LearnedModel *gm = model_of(wp, models);
+            const bool compact = gm && gm->n_heavy && gm->compact;
+            const uint32_t light = (ccnt[2 * w + right] + kTile - 1) / kTile;
+            if (kind == kWorkLight) c = compact ? light : 0u;
+            else if (kind == kWorkScatter) c = compact ? light : (wp.two_level ? 0u : tp[w + 1] - tp[w]);
+            else c = (wp.two_level && !compact) ? ip[w + 1] - ip[w] : 0u;
+        }
+        uint32_t tot;
+        const uint32_t ex = warp_excl_scan(c, &tot);
+        if (w < nwin) out[w] = carry + ex;
+        carry += tot;
+    }
+    if (lane_id() == 0) out[nwin] = carry;
+}
+
+// Work item t of a persistent pass over prefix arrays pl (left) / pr (right):
+// its window side and the index of the item inside the window side.
+struct WorkItem {
+    uint32_t w, local;
+    bool right;
+};
+__device__ __forceinline__ WorkItem work_item(const uint32_t *pl, const uint32_t *pr, uint32_t nwin, uint32_t t) {
+    WorkItem it;
+    it.right = t >= pl[nwin];
+    const uint32_t *p = it.right ? pr : pl;
+    const uint32_t x = it.right ? t - pl[nwin] : t;
+    it.w = find_window(p, nwin, x);
+    it.local = x - p[it.w];
+    return it;
+}
+
 __global__ void __launch_bounds__(kPartThreads)
 part_hist_light_kernel(const WinPlan *__restrict__ wins, uint32_t nwin, const uint32_t *__restrict__ tileL,
-                       const uint32_t *__restrict__ tileR, uint32_t *__restrict__ cnt, uint32_t B,
-                       const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
-                       const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt) {
+                       const uint32_t *__restrict__ tileR, const uint32_t *__restrict__ work,
+                       uint32_t *__restrict__ cnt, uint32_t B, const LearnedModel *__restrict__ models,
+                       const uint64_t *__restrict__ compL, const uint64_t *__restrict__ compR,
+                       const uint32_t *__restrict__ ccnt) {
     extern __shared__ uint32_t hist[];
     __shared__ LearnedCore core;
-    const uint32_t tilesL = tileL[nwin], tiles = tilesL + tileR[nwin];
-    for (uint32_t bt = blockIdx.x; bt < tiles; bt += gridDim.x) {
-        const bool right = bt >= tilesL;
-        const uint32_t t = right ? bt - tilesL : bt;
+    const uint32_t *pl = work + 2 * kWorkLight * (nwin + 1), *pr = pl + (nwin + 1);
+    const uint32_t items = pl[nwin] + pr[nwin];
+    for (uint32_t bt = blockIdx.x; bt < items; bt += gridDim.x) {
+        const WorkItem it = work_item(pl, pr, nwin, bt);
+        const bool right = it.right;
+        const uint32_t w = it.w;
         const uint32_t *tp = right ? tileR : tileL;
-        const uint32_t w = find_window(tp, nwin, t);
         const WinPlan wp = wins[w];
-        const LearnedModel *gm = model_of(wp, models);
-        if (!gm || !gm->n_heavy || !gm->compact) continue;   // uniform per CTA
+        const LearnedModel *gm = model_of(wp, models);   // a compacted window's model
         const uint64_t nside = ccnt[2 * w + (right ? 1 : 0)];
-        const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
-        if (start >= nside) continue;
+        const uint64_t start = (uint64_t)it.local * kTile;
         const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
         SJBG_BARRIER();   // the previous tile's readers of hist and core are done
         const Classifier cls = make_classifier(wp, gm, core);   // ends with a barrier
@@ -420,6 +475,72 @@ __global__ void __launch_bounds__(1024) part_scan_kernel(const uint32_t *__restr
     }
 }
 
+// Per window, one CTA: exclusive scan of the window's bucket counts on each
+// side, starting at the window's base in that side's partitioned array (the
+// tuples of the windows before it: baseL / baseR), giving the bucket starts
+// and scatter cursors; then every bucket with tuples on both sides is appended
+// to the join list (jlist, length *jn: nothing else can match).
+__global__ void __launch_bounds__(1024)
+part_scan_win_kernel(const WinPlan *__restrict__ wins, const uint32_t *__restrict__ baseL,
+                     const uint32_t *__restrict__ baseR, const uint32_t *__restrict__ cnt,
+                     uint32_t *__restrict__ start, uint32_t *__restrict__ cursor, uint32_t B,
+                     uint32_t *__restrict__ jlist, uint32_t *__restrict__ jn) {
+    __shared__ uint32_t warp_tot[32];
+    __shared__ uint32_t carry_s;
+    const uint32_t w = blockIdx.x;
+    const WinPlan wp = wins[w];
+    const uint32_t P = 1u << wp.log2_buckets, b0 = wp.bucket_base;
+    constexpr uint32_t kItems = 4;
+    const uint32_t chunk = blockDim.x * kItems;
+    for (uint32_t side = 0; side < 2; side++) {
+        const uint32_t lo = side * B + b0, hi = lo + P;
+        if (threadIdx.x == 0) carry_s = side ? baseR[w] : baseL[w];
+        SJBG_BARRIER();
+        for (uint32_t base = lo; base < hi; base += chunk) {
+            uint32_t v[kItems], s = 0;
+#pragma unroll
+            for (uint32_t k = 0; k < kItems; k++) {
+                const uint32_t i = base + threadIdx.x * kItems + k;
+                v[k] = i < hi ? cnt[i] : 0;
+                s += v[k];
+            }
+            uint32_t wt;
+            const uint32_t ex = warp_excl_scan(s, &wt);
+            if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
+            SJBG_BARRIER();
+            if (warp_id() == 0) {
+                const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0;
+                uint32_t tt;
+                warp_tot[lane_id()] = warp_excl_scan(x, &tt);
+            }
+            SJBG_BARRIER();
+            uint32_t run = carry_s + warp_tot[warp_id()] + ex;
+#pragma unroll
+            for (uint32_t k = 0; k < kItems; k++) {
+                const uint32_t i = base + threadIdx.x * kItems + k;
+                if (i < hi) {
+                    start[i] = run;
+                    cursor[i] = run;
+                }
+                run += v[k];
+            }
+            SJBG_BARRIER();
+            if (threadIdx.x == blockDim.x - 1) carry_s = run;
+            SJBG_BARRIER();
+        }
+    }
+    // join list: one reservation per warp of joinable buckets
+    for (uint32_t i0 = 0; i0 < P; i0 += blockDim.x) {
+        const uint32_t i = i0 + threadIdx.x, b = b0 + i;
+        const bool ok = i < P && cnt[b] != 0u && cnt[B + b] != 0u;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, ok);
+        uint32_t wbase = 0;
+        if (lane_id() == 0 && m) wbase = atomicAdd(jn, (uint32_t)__popc(m));
+        wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
+        if (ok) jlist[wbase + __popc(m & ((1u << lane_id()) - 1u))] = b;
+    }
+}
+
 // Block-wide exclusive scan of P (<= 16384) shared counters in place.
 __device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
     const uint32_t per = (P + blockDim.x - 1) / blockDim.x;
@@ -445,29 +566,24 @@ __device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
 }
 
 // ------------------------------------------------------------------ 3. scatter
-__device__ __forceinline__ void scatter_tile(uint32_t bt, const sjbg_tuple *__restrict__ L,
+__device__ __forceinline__ void scatter_tile(const WorkItem it, const sjbg_tuple *__restrict__ L,
                                              const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
-                                             uint32_t nwin, const uint32_t *__restrict__ tileL,
-                                             const uint32_t *__restrict__ tileR, uint32_t *__restrict__ cursor,
-                                             uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
-                                             const LearnedModel *__restrict__ models,
+                                             const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                                             uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL,
+                                             uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
                                              const uint64_t *__restrict__ compL, const uint64_t *__restrict__ compR,
-                                             const uint32_t *__restrict__ ccnt, bool skip_two_level) {
+                                             const uint32_t *__restrict__ ccnt) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t warp_tot[32];
-    const uint32_t tilesL = tileL[nwin];
-    const bool right = bt >= tilesL;
-    const uint32_t t = right ? bt - tilesL : bt;
+    const bool right = it.right;
+    const uint32_t w = it.w;
     const uint32_t *tp = right ? tileR : tileL;
-    const uint32_t w = find_window(tp, nwin, t);
     const WinPlan wp = wins[w];
     const LearnedModel *gm = model_of(wp, models);
     // compacted windows: the tiles cover the light tuples the counting pass wrote out
     const bool compact = gm && gm->n_heavy && gm->compact;
-    if (skip_two_level && !compact && wp.two_level) return;   // whole CTA: part_fine partitions this window
     const uint64_t nside = compact ? ccnt[2 * w + (right ? 1 : 0)] : (right ? wp.n_right : wp.n_left);
-    const uint64_t start = (uint64_t)(t - tp[w]) * kTile;
-    if (start >= nside) return;   // whole CTA
+    const uint64_t start = (uint64_t)it.local * kTile;
     const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
     const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
     const uint64_t *csrc = compact ? (right ? compR : compL) + (uint64_t)tp[w] * kTile + start : nullptr;
@@ -546,16 +662,17 @@ __device__ __forceinline__ void scatter_tile(uint32_t bt, const sjbg_tuple *__re
 __global__ void __launch_bounds__(kPartThreads, 3)
 part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                     uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
+                    const uint32_t *__restrict__ workL, const uint32_t *__restrict__ workR,
                     uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
                     const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
-                    const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt, bool skip_two_level) {
-    // persistent CTAs over the tiles of every window side (most tiles of
-    // compacted windows are past their packed light tuples and end at once)
-    const uint32_t tiles = tileL[nwin] + tileR[nwin];
-    for (uint32_t bt = blockIdx.x; bt < tiles; bt += gridDim.x) {
+                    const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt) {
+    // persistent CTAs over the tiles listed by the work prefixes workL / workR
+    // (a compacted window's light tiles; a single-level window's tiles)
+    const uint32_t items = workL[nwin] + workR[nwin];
+    for (uint32_t bt = blockIdx.x; bt < items; bt += gridDim.x) {
         SJBG_BARRIER();   // the previous tile's shared-memory readers are done
-        scatter_tile(bt, L, R, wins, nwin, tileL, tileR, cursor, B, outL, outR, models, compL, compR, ccnt,
-                     skip_two_level);
+        scatter_tile(work_item(workL, workR, nwin, bt), L, R, wins, tileL, tileR, cursor, B, outL, outR, models,
+                     compL, compR, ccnt);
     }
 }
 
@@ -568,7 +685,7 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
 // buckets: a local counting sort of up to kFineChunk tuples, one global
 // reservation per fine bucket, then contiguous per-bucket runs - coalesced
 // writes however many buckets the window has.  Persistent CTAs take the items
-// in turn; items of other windows end at once.
+// of the windows that need the pass (part_work's prefixes) in turn.
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
                  "l"(gmem)
@@ -578,9 +695,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 constexpr size_t kFineSmem = kFineChunk * (2 * sizeof(uint64_t) + sizeof(uint8_t));
 
-__device__ __forceinline__ void fine_item(uint32_t bi, const WinPlan *__restrict__ wins, uint32_t nwin,
+__device__ __forceinline__ void fine_item(const WorkItem it, const WinPlan *__restrict__ wins, uint32_t nwin,
                                           const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
-                                          const uint32_t *__restrict__ itemL, const uint32_t *__restrict__ itemR,
                                           uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL,
                                           uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
                                           const uint64_t *__restrict__ srcL, const uint64_t *__restrict__ srcR,
@@ -592,19 +708,15 @@ __device__ __forceinline__ void fine_item(uint32_t bi, const WinPlan *__restrict
     __shared__ uint32_t runoff[kGroupTiles], runpre[kGroupTiles + 1];
     __shared__ uint32_t fcnt[kCoarseMax], floc[kCoarseMax], fbase[kCoarseMax];
     __shared__ LearnedCore core;
-    const bool right = bi >= itemL[nwin];
-    const uint32_t item = right ? bi - itemL[nwin] : bi;
-    const uint32_t *ip = right ? itemR : itemL;
+    const bool right = it.right;
     const uint32_t *tp = right ? tileR : tileL;
-    const uint32_t w = find_window(ip, nwin, item);
+    const uint32_t w = it.w;
     const WinPlan wp = wins[w];
-    if (!wp.two_level) return;   // whole CTA
-    const LearnedModel *gm = model_of(wp, models);
-    if (gm && gm->n_heavy && gm->compact) return;   // compacted windows: part_scatter
+    const LearnedModel *gm = model_of(wp, models);   // a two-level window that was not compacted
     const uint32_t lg = wp.log2_buckets, lgC = coarse_bits(lg), cshift = lg - lgC, nfine = 1u << cshift;
     const uint32_t ntw = tp[w + 1] - tp[w];
     const uint32_t ngroups = (ntw + kGroupTiles - 1) / kGroupTiles;
-    const uint32_t local = item - ip[w];
+    const uint32_t local = it.local;
     const uint32_t c = local / ngroups, g = local % ngroups;
     const uint32_t t0 = g * kGroupTiles, G = min(kGroupTiles, ntw - t0);
     const Classifier cls = make_classifier(wp, gm, core);   // ends with a barrier when there is a model
@@ -705,15 +817,16 @@ __device__ __forceinline__ void fine_item(uint32_t bi, const WinPlan *__restrict
 
 __global__ void __launch_bounds__(kFineThreads, 4)
 part_fine_kernel(const WinPlan *__restrict__ wins, uint32_t nwin, const uint32_t *__restrict__ tileL,
-                 const uint32_t *__restrict__ tileR, const uint32_t *__restrict__ itemL,
-                 const uint32_t *__restrict__ itemR, uint32_t *__restrict__ cursor, uint32_t B,
-                 uint64_t *__restrict__ outL, uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
-                 const uint64_t *__restrict__ srcL, const uint64_t *__restrict__ srcR,
-                 const uint32_t *__restrict__ rows) {
-    const uint32_t items = itemL[nwin] + itemR[nwin];
+                 const uint32_t *__restrict__ tileR, const uint32_t *__restrict__ work, uint32_t *__restrict__ cursor,
+                 uint32_t B, uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
+                 const LearnedModel *__restrict__ models, const uint64_t *__restrict__ srcL,
+                 const uint64_t *__restrict__ srcR, const uint32_t *__restrict__ rows) {
+    const uint32_t *pl = work + 2 * kWorkFine * (nwin + 1), *pr = pl + (nwin + 1);
+    const uint32_t items = pl[nwin] + pr[nwin];
     for (uint32_t bi = blockIdx.x; bi < items; bi += gridDim.x) {
         SJBG_BARRIER();   // the previous item's shared-memory readers are done
-        fine_item(bi, wins, nwin, tileL, tileR, itemL, itemR, cursor, B, outL, outR, models, srcL, srcR, rows);
+        fine_item(work_item(pl, pr, nwin, bi), wins, nwin, tileL, tileR, cursor, B, outL, outR, models, srcL, srcR,
+                  rows);
     }
 }
 
@@ -990,15 +1103,19 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
     flush_acc(&acc[w], count, xr, prod);
 }
 
-// Bucket joins: one CTA per bucket (queue == nullptr) or persistent CTAs that
-// take buckets from a device work queue (an atomic counter) until it runs dry.
+// Bucket joins over the join list (jlist, length *jn; or, without a list,
+// buckets 0 .. B-1): one CTA per item (queue == nullptr) or persistent CTAs
+// that take items from a device work queue (an atomic counter) until it runs dry.
 __global__ void __launch_bounds__(kJoinThreads)
 bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
                          const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t cap,
-                         uint32_t *queue) {
+                         uint32_t *queue, const uint32_t *__restrict__ jlist, const uint32_t *__restrict__ jn) {
+    const uint32_t items = jlist ? *jn : B;
     if (!queue) {
-        join_count_bucket(blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc, cap);
+        if (blockIdx.x < items)
+            join_count_bucket(jlist ? jlist[blockIdx.x] : blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc,
+                              cap);
         return;
     }
     __shared__ uint32_t item_s;
@@ -1006,9 +1123,9 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
         SJBG_BARRIER();
         if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
         SJBG_BARRIER();
-        const uint32_t b = item_s;
-        if (b >= B) break;
-        join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, cap);
+        const uint32_t it = item_s;
+        if (it >= items) break;
+        join_count_bucket(jlist ? jlist[it] : it, partL, partR, start, cnt, B, bucket_win, acc, cap);
     }
 }
 
@@ -1017,9 +1134,12 @@ bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__re
                         const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc,
                         const WinPlan *__restrict__ wins, sjbg_pair *__restrict__ pairs, uint32_t table_bits,
-                        uint32_t *queue) {
+                        uint32_t *queue, const uint32_t *__restrict__ jlist, const uint32_t *__restrict__ jn) {
+    const uint32_t items = jlist ? *jn : B;
     if (!queue) {
-        join_enum_bucket(blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs, table_bits);
+        if (blockIdx.x < items)
+            join_enum_bucket(jlist ? jlist[blockIdx.x] : blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc,
+                             wins, pairs, table_bits);
         return;
     }
     __shared__ uint32_t item_s;
@@ -1027,9 +1147,10 @@ bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__re
         SJBG_BARRIER();
         if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
         SJBG_BARRIER();
-        const uint32_t b = item_s;
-        if (b >= B) break;
-        join_enum_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs, table_bits);
+        const uint32_t it = item_s;
+        if (it >= items) break;
+        join_enum_bucket(jlist ? jlist[it] : it, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs,
+                         table_bits);
     }
 }
 
@@ -1071,6 +1192,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     // ---- plan
     std::vector<WinPlan> plan(n);
     std::vector<uint32_t> tileL(n + 1), tileR(n + 1), hgL(n + 1), hgR(n + 1), itL(n + 1), itR(n + 1);
+    std::vector<uint32_t> pbL(n + 1), pbR(n + 1);   // window bases in the partitioned arrays
     uint64_t B = 0, totL = 0, totR = 0;
     uint32_t maxP = 1;
     bool any_two = false, any_one = false;
@@ -1103,6 +1225,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         itR[w + 1] = itR[w] + nc * ((tileR[w + 1] - tileR[w] + kGroupTiles - 1) / kGroupTiles);
         totL += wh.n_left;
         totR += wh.n_right;
+        pbL[w + 1] = (uint32_t)std::min<uint64_t>(totL, 0xFFFFFFFFull);
+        pbR[w + 1] = (uint32_t)std::min<uint64_t>(totR, 0xFFFFFFFFull);
     }
     if (B > 0xFFFFFFFFull / 4 || totL >= 0xFFFFFFFFull || totR >= 0xFFFFFFFFull)
         return fail(h, SJBG_E_CAPACITY, "hash join batch exceeds 2^32 tuples per side");
@@ -1112,7 +1236,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 
     // ---- upload plan, tile prefixes and bucket->window map in one copy
     const size_t planB = sizeof(WinPlan) * n, tileB = sizeof(uint32_t) * (n + 1), bwB = sizeof(uint32_t) * B;
-    const size_t upB = planB + 6 * tileB + bwB;
+    const size_t upB = planB + 8 * tileB + bwB;
     uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 0, upB));
     uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_WIN_PLAN, upB));
     if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "plan buffers");
@@ -1123,7 +1247,9 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     std::memcpy(hst + planB + 3 * tileB, hgR.data(), tileB);
     std::memcpy(hst + planB + 4 * tileB, itL.data(), tileB);
     std::memcpy(hst + planB + 5 * tileB, itR.data(), tileB);
-    std::memcpy(hst + planB + 6 * tileB, bwin.data(), bwB);
+    std::memcpy(hst + planB + 6 * tileB, pbL.data(), tileB);
+    std::memcpy(hst + planB + 7 * tileB, pbR.data(), tileB);
+    std::memcpy(hst + planB + 8 * tileB, bwin.data(), bwB);
     if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
     WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
     const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
@@ -1132,7 +1258,9 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     const uint32_t *dHgR = reinterpret_cast<const uint32_t *>(dev + planB + 3 * tileB);
     const uint32_t *dItL = reinterpret_cast<const uint32_t *>(dev + planB + 4 * tileB);
     const uint32_t *dItR = reinterpret_cast<const uint32_t *>(dev + planB + 5 * tileB);
-    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 6 * tileB);
+    const uint32_t *dPbL = reinterpret_cast<const uint32_t *>(dev + planB + 6 * tileB);
+    const uint32_t *dPbR = reinterpret_cast<const uint32_t *>(dev + planB + 7 * tileB);
+    const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 8 * tileB);
 
     uint32_t *dCnt = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CNT, sizeof(uint32_t) * 2 * B));
     uint32_t *dStart = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_START, sizeof(uint32_t) * 2 * B));
@@ -1156,9 +1284,14 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     const uint64_t tiles64 = (uint64_t)tileL[n] + tileR[n];
     uint64_t *dComp = static_cast<uint64_t *>(ws_get(h, WS_COMPACT, sizeof(uint64_t) * kTile * std::max<uint64_t>(tiles64, 1)));
     uint32_t *dRows = static_cast<uint32_t *>(ws_get(h, WS_COARSE_ROWS, sizeof(uint32_t) * kRow * std::max<uint64_t>(tiles64, 1)));
-    uint32_t *dCcnt = static_cast<uint32_t *>(ws_get(h, WS_COMPACT_CNT, sizeof(uint32_t) * 2 * n));
-    if (!dComp || !dRows || !dCcnt) return fail(h, SJBG_E_NOMEM, "partition staging buffers");
-    SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * 2 * n, h->stream));
+    // per window side its compacted light tuples, then the join list's length
+    uint32_t *dCcnt = static_cast<uint32_t *>(ws_get(h, WS_COMPACT_CNT, sizeof(uint32_t) * (2 * n + 1)));
+    uint32_t *dJn = dCcnt + 2 * n;
+    // the passes' work prefixes (6 arrays of n + 1), then the join list (B)
+    uint32_t *dWork = static_cast<uint32_t *>(ws_get(h, WS_TILE_PREFIX, sizeof(uint32_t) * (6 * (n + 1) + B)));
+    uint32_t *dJlist = dWork ? dWork + 6 * (n + 1) : nullptr;
+    if (!dComp || !dRows || !dCcnt || !dWork) return fail(h, SJBG_E_NOMEM, "partition staging buffers");
+    SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * (2 * n + 1), h->stream));
     uint64_t *dCompR = dComp + (uint64_t)kTile * tileL[n];
 
     SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
@@ -1172,32 +1305,38 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         if (learned)
             SJBG_CK(h, launch(h, "heavy_finish", heavy_finish_kernel, dim3(n), dim3(256), 0, (const WinPlan *)dPlan, n,
                               dModels, (const HeavyAcc *)dHeavy, acc));
+        // the tiles each later pass has work for (compacted windows: their light tiles only)
+        SJBG_CK(h, launch(h, "part_work", part_work_kernel, dim3(1), dim3(192), 0, (const WinPlan *)dPlan, n, dTileL,
+                          dTileR, dItL, dItR, dModels, (const uint32_t *)dCcnt, dWork));
         if (learned && !enumerate) {   // compacted windows exist only with heavy keys
             allow_big_smem(part_hist_light_kernel, sizeof(uint32_t) * maxP);
             const uint32_t lgrid = std::min<uint32_t>(tiles, 4u * (uint32_t)h->num_sms);
             SJBG_CK(h, launch(h, "part_hist_light", part_hist_light_kernel, dim3(lgrid), dim3(kPartThreads),
-                              sizeof(uint32_t) * maxP, (const WinPlan *)dPlan, n, dTileL, dTileR, dCnt, (uint32_t)B,
-                              dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dCcnt));
+                              sizeof(uint32_t) * maxP, (const WinPlan *)dPlan, n, dTileL, dTileR,
+                              (const uint32_t *)dWork, dCnt, (uint32_t)B, dModels, (const uint64_t *)dComp,
+                              (const uint64_t *)dCompR, (const uint32_t *)dCcnt));
         }
-        SJBG_CK(h, launch(h, "part_scan", part_scan_kernel, dim3(1), dim3(1024), 0, dCnt, dStart, dCur,
-                          (uint32_t)B));
+        SJBG_CK(h, launch(h, "part_scan", part_scan_win_kernel, dim3(n), dim3(1024), 0, (const WinPlan *)dPlan, dPbL,
+                          dPbR, (const uint32_t *)dCnt, dStart, dCur, (uint32_t)B, dJlist, dJn));
         // single-level windows, and compacted windows (their packed light tuples):
         // a local counting sort per tile
         if (any_one || (learned && !enumerate)) {
             const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;
             allow_big_smem(part_scatter_kernel, scatterSmem);
             const uint32_t sgrid = std::min<uint32_t>(tiles, 3u * 4u * (uint32_t)h->num_sms);
+            const uint32_t *wS = dWork + 2 * kWorkScatter * (n + 1);
             SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(sgrid), dim3(kPartThreads), scatterSmem,
-                              dL, dR, dPlan, n, dTileL, dTileR, dCur, (uint32_t)B, dPL, dPR, dModels,
-                              (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dCcnt, true));
+                              dL, dR, dPlan, n, dTileL, dTileR, wS, wS + (n + 1), dCur, (uint32_t)B, dPL, dPR,
+                              dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dCcnt));
         }
         // two-level windows: the fine pass over the tiles' coarse runs
         if (any_two && itL[n] + itR[n]) {
             allow_big_smem(part_fine_kernel, kFineSmem);
             const uint32_t fgrid = std::min<uint32_t>(itL[n] + itR[n], 4u * 4u * (uint32_t)h->num_sms);
             SJBG_CK(h, launch(h, "part_fine", part_fine_kernel, dim3(fgrid), dim3(kFineThreads), kFineSmem,
-                              (const WinPlan *)dPlan, n, dTileL, dTileR, dItL, dItR, dCur, (uint32_t)B, dPL, dPR,
-                              dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dRows));
+                              (const WinPlan *)dPlan, n, dTileL, dTileR, (const uint32_t *)dWork, dCur, (uint32_t)B,
+                              dPL, dPR, dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR,
+                              (const uint32_t *)dRows));
         }
     }
     // persistent CTAs draining a work queue of buckets, or one CTA per bucket
@@ -1215,7 +1354,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         const size_t smem = sizeof(uint32_t) * (2 * ((1u << bits) + 1) + 2 * kEnumChunk);
         allow_big_smem(bucket_join_enum_kernel, smem);
         SJBG_CK(h, launch(h, "bucket_join_enum", bucket_join_enum_kernel, jgrid, dim3(kJoinThreads), smem,
-                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits, queue));
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits, queue,
+                          (const uint32_t *)dJlist, (const uint32_t *)dJn));
     } else {
         const uint32_t cap = count_table_cap((uint32_t)target);
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
@@ -1225,7 +1365,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
             jgrid = dim3((uint32_t)std::min<uint64_t>(B, (uint64_t)h->num_sms * std::min<uint32_t>(per_sm, 2u)));
         }
         SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, jgrid, dim3(kJoinThreads), smem,
-                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, cap, queue));
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, cap, queue, (const uint32_t *)dJlist,
+                          (const uint32_t *)dJn));
     }
     return SJBG_OK;
 }
@@ -1312,13 +1453,15 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * P;
         allow_big_smem(part_scatter_kernel, scatterSmem);
-        part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, cur, P, pL,
-                                                                          pR, nullptr, nullptr, nullptr, nullptr,
-                                                                          false);
+        // a single-level radix window: the scatter work is every tile
+        part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, tl, tl + 2,
+                                                                          cur, P, pL, pR, nullptr, nullptr, nullptr,
+                                                                          nullptr);
         const uint32_t cap = count_table_cap(4096);
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
-        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, cap, nullptr);
+        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, cap, nullptr,
+                                                                nullptr, nullptr);
     }
     raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);
     return cudaGetLastError() == cudaSuccess ? SJBG_OK : SJBG_E_CUDA;
