@@ -3,11 +3,14 @@
 //
 // Per window, on the device:
 //   1. sample      rate * (|L|+|R|) keys at jittered strided positions of both
-//                  sides; per-window min/max key.
+//                  sides, gathered once into a packed key array; per-window
+//                  min/max key.
 //   2. count       equal-width histogram of the sample over kBins key bins and
-//                  exact per-key sample counts in a per-window hash table.
-//   3. heavy       keys whose sample count exceeds one bucket's fair share
-//                  become candidates.
+//                  exact per-key sample counts in a per-window hash table; the
+//                  keys reaching the candidate threshold are listed and the
+//                  listed keys are counted per count class as they grow.
+//   3. heavy       listed keys whose sample count exceeds one bucket's fair
+//                  share become candidates.
 //   4. fit         (one CTA per window) the top kMaxHeavy candidates are made
 //                  heavy and removed from the histogram; the light CDF at the
 //                  bin edges is fitted by least squares: a root line routes
@@ -37,35 +40,68 @@ struct SampleWin {
     uint64_t table_off;    // first slot of this window's table
     uint32_t thresh;       // heavy candidate threshold (sample count)
     uint32_t log2_buckets;
+    uint32_t run_log2;     // samples are runs of 2^run_log2 consecutive tuples (3, or 0 for tiny windows)
+    uint32_t pad0;
+    uint64_t key_off;      // first sampled key of this window in the packed key array
+    uint64_t list_off;     // first entry of this window's list of keys at or above thresh
+    uint32_t list_cap;     // m / thresh + 1: every listed key has at least thresh samples
+    uint32_t pad;
 };
 
 struct SampleScratch {
     uint32_t kmin, kmax;   // sample key range
     uint32_t n_cand;
     uint32_t cut;          // candidates have a sample count >= cut
-    uint32_t cls[32];      // candidate keys per count class floor(log2(count))
+    uint32_t cls[32];      // listed keys per count class floor(log2(count))
+    uint32_t n_list;       // keys that reached thresh (table slots in the list)
+    uint32_t pad[3];
 };
 
+// Sample i of a window: the samples come in runs of 2^run_log2 consecutive
+// tuples (one 128-byte line for runs of 8), even runs from the left side, odd
+// from the right; the j-th run of a side lies in the j-th of its equal strides,
+// at a hashed offset inside it (the high half of hash * room: no division).
 __device__ __forceinline__ uint32_t sample_key(const SampleWin &s, const sjbg_tuple *L, const sjbg_tuple *R, uint32_t i) {
-    const bool right = i & 1u;
+    const uint32_t run = 1u << s.run_log2;
+    const uint32_t r = i >> s.run_log2, q = i & (run - 1u);
+    const bool right = r & 1u;
     const uint64_t n = right ? s.n_right : s.n_left;
-    const uint64_t half = s.m >> 1;
-    const uint64_t j = i >> 1;
-    const uint64_t stride = n / half;   // >= 1 by construction of m
-    uint64_t idx = j * stride + (stride > 1 ? sjbg_mix64(0x5A17ull + i) % stride : 0);
+    const uint64_t runs = s.m >> (s.run_log2 + 1);   // runs per side
+    const uint64_t j = r >> 1;
+    const uint64_t stride = n / runs;   // >= run by construction of m, < 2^32 for n < 2^36
+    const uint64_t room = stride - run + 1;
+    const uint64_t jit = ((uint64_t)(uint32_t)sjbg_mix64(0x5A17ull + r) * (room & 0xFFFFFFFFull)) >> 32;
+    uint64_t idx = j * stride + jit + q;
     if (idx >= n) idx = n - 1;
     return right ? R[s.right_off + idx].key : L[s.left_off + idx].key;
 }
 
+// Gathers each window's sample into the packed key array (four independent
+// loads per thread in flight) and its min/max key.
 __global__ void __launch_bounds__(kSampleThreads)
-sample_minmax_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *wins, SampleScratch *scr) {
+sample_minmax_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *wins, SampleScratch *scr,
+                     uint32_t *keys) {
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
+    uint32_t *kw = keys + s.key_off;
     uint32_t lo = 0xFFFFFFFFu, hi = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.m; i += gridDim.x * blockDim.x) {
-        uint32_t k = sample_key(s, L, R, i);
-        lo = min(lo, k);
-        hi = max(hi, k);
+    const uint32_t step = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < s.m; i0 += 4 * step) {
+        uint32_t k[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t i = i0 + q * step;
+            k[q] = i < s.m ? sample_key(s, L, R, i) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t i = i0 + q * step;
+            if (i < s.m) {
+                kw[i] = k[q];
+                lo = min(lo, k[q]);
+                hi = max(hi, k[q]);
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
@@ -91,56 +127,100 @@ __device__ __forceinline__ uint32_t bin_of(float x) {
 }
 
 // Sample histogram + exact sample counts (table slot = key << 32 | count).
-__global__ void __launch_bounds__(kSampleThreads)
-sample_count_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *wins, const SampleScratch *scr,
-                    uint32_t *hist, unsigned long long *table) {
-    const uint32_t w = blockIdx.y;
-    const SampleWin s = wins[w];
-    float kmin, inv;
-    model_range(scr[w], &kmin, &inv);
-    uint32_t *hw = hist + (uint64_t)w * kBins;
-    unsigned long long *tw = table + s.table_off;
+// A CTA aggregates kCountChunk sampled keys at a time in a shared table, then
+// adds each distinct key's count once to the window's histogram and table.
+// Each table update moves its key between count classes; a key's updates are
+// ordered by the atomics, so every class change is counted exactly once, and
+// the update that lifts a key to thresh lists its slot.
+constexpr uint32_t kCountChunk = 2048;
+constexpr uint32_t kCountSlotsLog2 = 12;   // 2 * kCountChunk slots: a free slot always exists
+constexpr uint32_t kCountSlots = 1u << kCountSlotsLog2;
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;   // empty shared slot (the key itself counts in slot kCountSlots)
+
+__device__ __forceinline__ void count_update(const SampleWin &s, SampleScratch &sc, uint32_t *hw,
+                                             unsigned long long *tw, uint32_t *lw, float kmin, float inv, uint32_t k,
+                                             uint32_t c) {
     const uint32_t mask = (1u << s.table_log2) - 1;
-    // warp-uniform trip count: equal sampled keys of a warp are combined first,
-    // so a hot key costs one atomic per warp instead of one per sample
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + warp_id()) * 32; base < s.m; base += warps * 32) {
-        const uint32_t i = base + lane_id();
-        const bool valid = i < s.m;
-        const uint32_t k = valid ? sample_key(s, L, R, i) : 0u;
-        const unsigned active = __ballot_sync(0xFFFFFFFFu, valid);
-        const unsigned grp = __match_any_sync(0xFFFFFFFFu, k) & active;
-        if (!valid || (int)lane_id() != __ffs(grp) - 1) continue;
-        const uint32_t c = __popc(grp);
-        atomicAdd(&hw[bin_of(key_x(k, kmin, inv))], c);
-        uint32_t slot = slot_hash(k, s.table_log2);
-        for (uint32_t p = 0; p <= mask; p++) {
-            unsigned long long cur = tw[slot];
-            if (cur == 0ull) {
-                unsigned long long prev = atomicCAS(&tw[slot], 0ull, ((unsigned long long)k << 32) | c);
-                if (prev == 0ull) break;
-                cur = prev;
-            }
-            if ((uint32_t)(cur >> 32) == k) {
-                atomicAdd(&tw[slot], (unsigned long long)c);
+    atomicAdd(&hw[bin_of(key_x(k, kmin, inv))], c);
+    uint32_t slot = slot_hash(k, s.table_log2);
+    uint32_t before = 0xFFFFFFFFu;   // the key's count before this update
+    for (uint32_t p = 0; p <= mask; p++) {
+        unsigned long long cur = tw[slot];
+        if (cur == 0ull) {
+            unsigned long long prev = atomicCAS(&tw[slot], 0ull, ((unsigned long long)k << 32) | c);
+            if (prev == 0ull) {
+                before = 0;
                 break;
             }
-            slot = (slot + 1) & mask;
+            cur = prev;
+        }
+        if ((uint32_t)(cur >> 32) == k) {
+            before = (uint32_t)atomicAdd(&tw[slot], (unsigned long long)c);
+            break;
+        }
+        slot = (slot + 1) & mask;
+    }
+    const uint32_t after = before + c;
+    if (before == 0xFFFFFFFFu || after < s.thresh) return;   // (a full table drops the key)
+    const int cn = 31 - __clz(after);
+    if (before < s.thresh) {
+        atomicAdd(&sc.cls[cn], 1u);
+        const uint32_t pos = atomicAdd(&sc.n_list, 1u);
+        if (pos < s.list_cap) lw[pos] = slot;
+    } else {
+        const int co = 31 - __clz(before);
+        if (co != cn) {
+            atomicAdd(&sc.cls[cn], 1u);
+            atomicSub(&sc.cls[co], 1u);
         }
     }
 }
 
-// Candidates per count class, so that the candidate cut keeps the heaviest keys.
 __global__ void __launch_bounds__(kSampleThreads)
-heavy_classes_kernel(const SampleWin *wins, const unsigned long long *table, SampleScratch *scr) {
+sample_count_kernel(const uint32_t *keys, const SampleWin *wins, SampleScratch *scr, uint32_t *hist,
+                    unsigned long long *table, uint32_t *lists) {
+    __shared__ uint32_t skey[kCountSlots], scnt[kCountSlots + 1];
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
-    const unsigned long long *tw = table + s.table_off;
-    const uint32_t slots = 1u << s.table_log2;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
-        const unsigned long long v = tw[i];
-        const uint32_t c = (uint32_t)v;
-        if (v && c >= s.thresh) atomicAdd(&scr[w].cls[31 - __clz(c)], 1u);
+    float kmin, inv;
+    model_range(scr[w], &kmin, &inv);
+    const uint32_t *kw = keys + s.key_off;
+    uint32_t *hw = hist + (uint64_t)w * kBins;
+    uint32_t *lw = lists + s.list_off;
+    SampleScratch &sc = scr[w];
+    unsigned long long *tw = table + s.table_off;
+    for (uint32_t j = threadIdx.x; j <= kCountSlots; j += blockDim.x) {
+        if (j < kCountSlots) skey[j] = kNoKey;
+        scnt[j] = 0;
+    }
+    SJBG_BARRIER();
+    for (uint32_t base = blockIdx.x * kCountChunk; base < s.m; base += gridDim.x * kCountChunk) {
+        const uint32_t end = min(base + kCountChunk, s.m);
+        for (uint32_t i = base + threadIdx.x; i < end; i += blockDim.x) {
+            const uint32_t k = kw[i];
+            if (k == kNoKey) {
+                atomicAdd(&scnt[kCountSlots], 1u);
+                continue;
+            }
+            uint32_t slot = slot_hash(k, kCountSlotsLog2);
+            for (uint32_t p = 0; p < kCountSlots; p++) {
+                const uint32_t prev = atomicCAS(&skey[slot], kNoKey, k);
+                if (prev == kNoKey || prev == k) {
+                    atomicAdd(&scnt[slot], 1u);
+                    break;
+                }
+                slot = (slot + 1) & (kCountSlots - 1);
+            }
+        }
+        SJBG_BARRIER();
+        for (uint32_t j = threadIdx.x; j <= kCountSlots; j += blockDim.x) {
+            const uint32_t c = scnt[j];
+            if (!c) continue;
+            count_update(s, sc, hw, tw, lw, kmin, inv, j < kCountSlots ? skey[j] : kNoKey, c);
+            if (j < kCountSlots) skey[j] = kNoKey;
+            scnt[j] = 0;
+        }
+        SJBG_BARRIER();
     }
 }
 
@@ -155,17 +235,19 @@ __device__ __forceinline__ uint32_t candidate_cut(const SampleScratch &sc, uint3
     return thresh;
 }
 
+// The listed keys (those that reached thresh) at or above the cut.
 __global__ void __launch_bounds__(kSampleThreads)
 heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, SampleScratch *scr,
-                        unsigned long long *cand) {
+                        const uint32_t *lists, unsigned long long *cand) {
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
     const unsigned long long *tw = table + s.table_off;
-    const uint32_t slots = 1u << s.table_log2;
+    const uint32_t *lw = lists + s.list_off;
+    const uint32_t nl = min(scr[w].n_list, s.list_cap);
     const uint32_t cut = candidate_cut(scr[w], s.thresh);
     if (blockIdx.x == 0 && threadIdx.x == 0) scr[w].cut = cut;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += gridDim.x * blockDim.x) {
-        const unsigned long long v = tw[i];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x) {
+        const unsigned long long v = tw[lw[i]];
         const uint32_t c = (uint32_t)v;
         if (v && c >= cut) {
             uint32_t pos = atomicAdd(&scr[w].n_cand, 1u);
@@ -187,6 +269,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     __shared__ double rootpart[32][2];
     __shared__ float root_s[2];
     __shared__ uint32_t n_heavy_s, light_total_s, log2_eff_s, compact_s;
+    __shared__ uint32_t cpre[kCandMax + 1];        // exclusive prefix of the sorted candidates' counts
     const uint32_t w = blockIdx.x;
     const SampleWin s = wins[w];
     LearnedModel &M = models[w];
@@ -198,9 +281,13 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     const uint32_t nc = min(scr[w].n_cand, kCandMax);
     for (uint32_t i = threadIdx.x; i < kCandMax; i += blockDim.x) sc[i] = i < nc ? cand[(uint64_t)w * kCandMax + i] : 0ull;
     SJBG_BARRIER();
-    for (uint32_t k = 2; k <= kCandMax; k <<= 1) {
+    // only the first ncap (the candidates, rounded up to a power of two) take
+    // part: the rest are zeros and already in place
+    uint32_t ncap = 2;
+    while (ncap < nc) ncap <<= 1;
+    for (uint32_t k = 2; k <= ncap; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < kCandMax; i += blockDim.x) {
+            for (uint32_t i = threadIdx.x; i < ncap; i += blockDim.x) {
                 const uint32_t p = i ^ j;
                 if (p > i) {
                     const bool desc = (i & k) == 0;
@@ -211,20 +298,40 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             SJBG_BARRIER();
         }
     }
-    if (threadIdx.x == 0) {
-        // largest first, a candidate is heavy while its sampled count exceeds an
-        // eighth of one bucket's share of the mass that is still light
-        const uint64_t P = 1ull << s.log2_buckets;
-        uint64_t light = s.m;
-        uint32_t h = 0;
-        const uint32_t lim = min(nc, max_heavy);
-        while (h < lim) {
-            const uint64_t c = sc[h] >> 32;
-            if (c * 8 * P <= light) break;
-            light -= c;
-            h++;
+    // largest first, a candidate is heavy while its sampled count exceeds an
+    // eighth of one bucket's share of the mass that is still light: the first
+    // h with c_h * 8P <= m - (c_0 + .. + c_{h-1}) ends the heavy keys
+    const uint64_t P = 1ull << s.log2_buckets;
+    const uint32_t lim = min(nc, max_heavy);
+    {
+        const uint32_t per = kCandMax / blockDim.x, h0 = threadIdx.x * per;   // 2 candidates per thread
+        uint32_t sum = 0;
+        for (uint32_t q = 0; q < per; q++) sum += (uint32_t)(sc[h0 + q] >> 32);
+        uint32_t tot;
+        const uint32_t ex = warp_excl_scan(sum, &tot);
+        if (lane_id() == 31) warp_tot[warp_id()] = ex + sum;
+        if (threadIdx.x == 0) n_heavy_s = lim;
+        SJBG_BARRIER();
+        if (warp_id() == 0) {
+            const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0u;
+            uint32_t tt;
+            warp_tot[lane_id()] = warp_excl_scan(x, &tt);
+            if (lane_id() == 0) cpre[kCandMax] = tt;
         }
-        n_heavy_s = h;
+        SJBG_BARRIER();
+        uint32_t run = warp_tot[warp_id()] + ex;
+        for (uint32_t q = 0; q < per; q++) {
+            const uint32_t h = h0 + q;
+            const uint32_t c = (uint32_t)(sc[h] >> 32);
+            cpre[h] = run;
+            if (h < lim && (uint64_t)c * 8 * P <= (uint64_t)s.m - run) atomicMin(&n_heavy_s, h);
+            run += c;
+        }
+        SJBG_BARRIER();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t h = n_heavy_s;
+        const uint64_t light = (uint64_t)s.m - cpre[h];
         // fan-out for the light keys only: about as many light tuples per
         // bucket as the window's plan has tuples per bucket
         uint32_t lg = s.log2_buckets;
@@ -401,8 +508,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
 
 // Inference on the sample: predicted bucket sizes of the light keys.
 __global__ void __launch_bounds__(kSampleThreads)
-learned_check_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *wins, const LearnedModel *models,
-                     uint32_t *pred) {
+learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedModel *models, uint32_t *pred) {
     __shared__ HeavySet hs;
     __shared__ LearnedCore core;
     const uint32_t w = blockIdx.y;
@@ -412,8 +518,9 @@ learned_check_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *
     heavy_set_load(hs, m);
     copy_to_smem(&core, m, sizeof(LearnedCore));
     uint32_t *pw = pred + (uint64_t)w * kPredStride;
+    const uint32_t *kw = keys + s.key_off;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.m; i += gridDim.x * blockDim.x) {
-        const uint32_t k = sample_key(s, L, R, i);
+        const uint32_t k = kw[i];
         if (heavy_find(hs, k) != kHeavyBucket) continue;
         atomicAdd(&pw[learned_bucket(core, k)], 1u);
     }
@@ -460,8 +567,8 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     const float bound = h->cfg.overflow_bound > 0.0f ? h->cfg.overflow_bound : 8.0f;
     const uint32_t leaves = h->cfg.learned_leaves ? std::min(h->cfg.learned_leaves, kMaxLeaves) : kMaxLeaves;
     std::vector<SampleWin> sw(n);
-    uint64_t table_total = 0;
-    uint32_t max_m = 0;
+    uint64_t table_total = 0, keys_total = 0, list_total = 0;
+    uint32_t max_m = 0, max_list = 0;
     for (uint32_t w = 0; w < n; w++) {
         const WinPlan &p = plan[w];
         SampleWin &s = sw[w];
@@ -470,7 +577,11 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         uint64_t m = (uint64_t)((double)rate * (double)(p.n_left + p.n_right));
         m = std::max<uint64_t>(m, 64);
         m = std::min<uint64_t>(m, 2 * nmin);   // at most one sample per tuple
-        m &= ~1ull;
+        // runs of 8 tuples (whole 128-byte lines) once each side has room for
+        // 8 runs: m a multiple of 16 samples, at most one per tuple
+        s.run_log2 = (m >= 128 && nmin >= 64) ? 3u : 0u;
+        s.pad0 = 0;
+        m &= ~((2ull << s.run_log2) - 1);
         if (nmin == 0) m = 0;
         s.m = (uint32_t)m;
         uint32_t lg = 6;
@@ -483,7 +594,14 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         // heavy candidates: keys sampled at least max(4, m / 64P) times; the fit
         // keeps those that exceed an eighth of a bucket of the remaining light mass
         s.thresh = (uint32_t)std::max<uint64_t>(4, m / (64 * P));
+        s.key_off = keys_total;
+        keys_total += m;
+        s.list_cap = (uint32_t)(m / s.thresh + 1);
+        s.list_off = list_total;
+        list_total += s.list_cap;
+        s.pad = 0;
         max_m = std::max(max_m, s.m);
+        max_list = std::max(max_list, s.list_cap);
     }
     const size_t swB = sizeof(SampleWin) * n, scB = sizeof(SampleScratch) * n;
     const size_t histB = sizeof(uint32_t) * (size_t)kBins * n, tabB = sizeof(unsigned long long) * table_total;
@@ -494,7 +612,11 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     unsigned long long *dTab = static_cast<unsigned long long *>(ws_get(h, WS_AUX1, tabB));
     unsigned long long *dCand = static_cast<unsigned long long *>(ws_get(h, WS_AUX2, candB));
     LearnedModel *dM = static_cast<LearnedModel *>(ws_get(h, WS_MODEL, sizeof(LearnedModel) * n));
-    if (!hst || !dsmall || !dHist || !dTab || !dCand || !dM) return fail(h, SJBG_E_NOMEM, "learned partitioner buffers");
+    // the packed sample keys of every window, then the windows' lists of keys at or above thresh
+    uint32_t *dKeys = static_cast<uint32_t *>(ws_get(h, WS_SAMPLE_KEYS, sizeof(uint32_t) * (keys_total + list_total + 1)));
+    if (!hst || !dsmall || !dHist || !dTab || !dCand || !dM || !dKeys)
+        return fail(h, SJBG_E_NOMEM, "learned partitioner buffers");
+    uint32_t *dLists = dKeys + keys_total;
     uint32_t *dPred = dHist + (size_t)kBins * n;
     std::memcpy(hst, sw.data(), swB);
     SampleScratch init;
@@ -508,21 +630,21 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     const SampleWin *dSw = reinterpret_cast<const SampleWin *>(dsmall);
     SampleScratch *dScr = reinterpret_cast<SampleScratch *>(dsmall + swB);
 
-    const uint32_t bx = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 4095) / 4096));
-    const dim3 g(bx, n);
-    SJBG_CK(h, launch(h, "learned_sample", sample_minmax_kernel, g, dim3(kSampleThreads), 0, dL, dR, dSw, dScr));
-    SJBG_CK(h, launch(h, "learned_count", sample_count_kernel, g, dim3(kSampleThreads), 0, dL, dR, dSw,
-                      (const SampleScratch *)dScr, dHist, dTab));
-    const uint32_t tx = std::max<uint32_t>(1, std::min<uint32_t>(64, (uint32_t)((table_total / n + 4095) / 4096)));
-    SJBG_CK(h, launch(h, "learned_classes", heavy_classes_kernel, dim3(tx, n), dim3(kSampleThreads), 0, dSw,
-                      (const unsigned long long *)dTab, dScr));
+    const uint32_t bs = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 16383) / 16384));
+    SJBG_CK(h, launch(h, "learned_sample", sample_minmax_kernel, dim3(bs, n), dim3(kSampleThreads), 0, dL, dR, dSw,
+                      dScr, dKeys));
+    const uint32_t bn = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 2 * kCountChunk - 1) / (2 * kCountChunk)));
+    SJBG_CK(h, launch(h, "learned_count", sample_count_kernel, dim3(bn, n), dim3(kSampleThreads), 0,
+                      (const uint32_t *)dKeys, dSw, dScr, dHist, dTab, dLists));
+    const uint32_t tx = std::max<uint32_t>(1, std::min<uint32_t>(16, (max_list + 4095) / 4096));
     SJBG_CK(h, launch(h, "learned_heavy", heavy_candidates_kernel, dim3(tx, n), dim3(kSampleThreads), 0, dSw,
-                      (const unsigned long long *)dTab, dScr, dCand));
+                      (const unsigned long long *)dTab, dScr, (const uint32_t *)dLists, dCand));
     allow_big_smem(learned_fit_kernel, sizeof(uint32_t) * kBins);
     SJBG_CK(h, launch(h, "learned_fit", learned_fit_kernel, dim3(n), dim3(1024), sizeof(uint32_t) * kBins, dSw, dScr,
                       dHist, dCand, dM, leaves, allow_heavy ? kMaxHeavy : 0u, bound));
-    SJBG_CK(h, launch(h, "learned_check", learned_check_kernel, g, dim3(kSampleThreads), 0, dL, dR, dSw,
-                      (const LearnedModel *)dM, dPred));
+    const uint32_t bc = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 4095) / 4096));
+    SJBG_CK(h, launch(h, "learned_check", learned_check_kernel, dim3(bc, n), dim3(kSampleThreads), 0,
+                      (const uint32_t *)dKeys, dSw, (const LearnedModel *)dM, dPred));
     SJBG_CK(h, launch(h, "learned_overflow", learned_overflow_kernel, dim3(n), dim3(1024), 0, dSw, dM,
                       (const uint32_t *)dPred, bound));
     SJBG_CK(h, launch(h, "learned_set_model", set_model_kernel, dim3((n + 255) / 256), dim3(256), 0, dPlan, n));
