@@ -281,22 +281,47 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     const uint32_t nc = min(scr[w].n_cand, kCandMax);
     for (uint32_t i = threadIdx.x; i < kCandMax; i += blockDim.x) sc[i] = i < nc ? cand[(uint64_t)w * kCandMax + i] : 0ull;
     SJBG_BARRIER();
-    // only the first ncap (the candidates, rounded up to a power of two) take
-    // part: the rest are zeros and already in place
-    uint32_t ncap = 2;
-    while (ncap < nc) ncap <<= 1;
-    for (uint32_t k = 2; k <= ncap; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < ncap; i += blockDim.x) {
-                const uint32_t p = i ^ j;
-                if (p > i) {
-                    const bool desc = (i & k) == 0;
-                    const unsigned long long a = sc[i], b = sc[p];
-                    if (desc ? (a < b) : (a > b)) { sc[i] = b; sc[p] = a; }
+    // Thread t holds elements t and t + 1024 in registers.  Stages up to
+    // ncap (the candidates rounded up to a power of two: the zeros beyond it
+    // only meet zeros); partners j < 32 apart are exchanged by warp shuffles,
+    // j = 1024 inside the thread, the others through shared memory.
+    {
+        static_assert(kCandMax == 2048, "two sort elements per thread of 1024");
+        uint32_t ncap = 2;
+        while (ncap < nc) ncap <<= 1;
+        const uint32_t t = threadIdx.x;
+        unsigned long long v0 = sc[t], v1 = sc[t + 1024];
+        // element i with partner value pv: the lower index of a descending
+        // pair (and the upper of an ascending one) keeps the larger value
+        auto cx = [](unsigned long long v, unsigned long long pv, uint32_t i, uint32_t j, uint32_t k) {
+            const bool lower = (i & j) == 0, desc = (i & k) == 0;
+            return (lower == desc) ? (v > pv ? v : pv) : (v < pv ? v : pv);
+        };
+        for (uint32_t k = 2; k <= ncap; k <<= 1) {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                if (j == 1024) {   // k = 2048: descending, element t is the lower one
+                    const unsigned long long hi = v0 > v1 ? v0 : v1, lo = v0 > v1 ? v1 : v0;
+                    v0 = hi;
+                    v1 = lo;
+                } else if (j >= 32) {
+                    sc[t] = v0;
+                    sc[t + 1024] = v1;
+                    SJBG_BARRIER();
+                    const unsigned long long p0 = sc[t ^ j], p1 = sc[(t ^ j) + 1024];
+                    SJBG_BARRIER();
+                    v0 = cx(v0, p0, t, j, k);
+                    v1 = cx(v1, p1, t + 1024, j, k);
+                } else {
+                    const unsigned long long p0 = __shfl_xor_sync(0xFFFFFFFFu, v0, j);
+                    const unsigned long long p1 = __shfl_xor_sync(0xFFFFFFFFu, v1, j);
+                    v0 = cx(v0, p0, t, j, k);
+                    v1 = cx(v1, p1, t + 1024, j, k);
                 }
             }
-            SJBG_BARRIER();
         }
+        sc[t] = v0;
+        sc[t + 1024] = v1;
+        SJBG_BARRIER();
     }
     // largest first, a candidate is heavy while its sampled count exceeds an
     // eighth of one bucket's share of the mass that is still light: the first
@@ -526,12 +551,15 @@ learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedM
     }
 }
 
-// One CTA per window: worst predicted bucket vs the mean -> fallback flag.
+// One CTA per window: worst predicted bucket vs the mean -> fallback flag;
+// the window's plan is pointed at its model slot.
 __global__ void __launch_bounds__(1024)
-learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint32_t *pred, float bound) {
+learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint32_t *pred, float bound,
+                        WinPlan *plan) {
     __shared__ uint32_t mx_s, sum_s;
     const uint32_t w = blockIdx.x;
     LearnedModel &M = models[w];
+    if (threadIdx.x == 0) plan[w].model = w;
     if (M.fallback) return;
     if (threadIdx.x == 0) { mx_s = 0; sum_s = 0; }
     SJBG_BARRIER();
@@ -547,11 +575,6 @@ learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint3
         // a window whose light sample is too small to judge keeps its model
         if (sum_s >= 4 * P && (float)mx_s > bound * mean) M.fallback = 1u;
     }
-}
-
-__global__ void set_model_kernel(WinPlan *plan, uint32_t n) {
-    uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w < n) plan[w].model = w;
 }
 
 uint32_t learned_log2_buckets(sjbg_handle *h, uint64_t n_left) {
@@ -630,10 +653,11 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     const SampleWin *dSw = reinterpret_cast<const SampleWin *>(dsmall);
     SampleScratch *dScr = reinterpret_cast<SampleScratch *>(dsmall + swB);
 
-    const uint32_t bs = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 16383) / 16384));
+    // one pass of four loads per thread: all of a window's sample in flight at once
+    const uint32_t bs = std::max<uint32_t>(1, std::min<uint32_t>(256, (max_m + 1023) / 1024));
     SJBG_CK(h, launch(h, "learned_sample", sample_minmax_kernel, dim3(bs, n), dim3(kSampleThreads), 0, dL, dR, dSw,
                       dScr, dKeys));
-    const uint32_t bn = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 2 * kCountChunk - 1) / (2 * kCountChunk)));
+    const uint32_t bn = std::max<uint32_t>(1, std::min<uint32_t>(256, (max_m + kCountChunk - 1) / kCountChunk));
     SJBG_CK(h, launch(h, "learned_count", sample_count_kernel, dim3(bn, n), dim3(kSampleThreads), 0,
                       (const uint32_t *)dKeys, dSw, dScr, dHist, dTab, dLists));
     const uint32_t tx = std::max<uint32_t>(1, std::min<uint32_t>(16, (max_list + 4095) / 4096));
@@ -646,8 +670,7 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     SJBG_CK(h, launch(h, "learned_check", learned_check_kernel, dim3(bc, n), dim3(kSampleThreads), 0,
                       (const uint32_t *)dKeys, dSw, (const LearnedModel *)dM, dPred));
     SJBG_CK(h, launch(h, "learned_overflow", learned_overflow_kernel, dim3(n), dim3(1024), 0, dSw, dM,
-                      (const uint32_t *)dPred, bound));
-    SJBG_CK(h, launch(h, "learned_set_model", set_model_kernel, dim3((n + 255) / 256), dim3(256), 0, dPlan, n));
+                      (const uint32_t *)dPred, bound, dPlan));
     *dModels = dM;
     return SJBG_OK;
 }
