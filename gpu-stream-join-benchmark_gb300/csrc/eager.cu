@@ -74,7 +74,7 @@ __device__ __forceinline__ uint32_t etab_claim(const ETab &t, uint32_t key) {
 }
 
 __device__ __forceinline__ unsigned long long own_hash(int side, uint32_t val) {
-    return side == 0 ? sjbg_fr(val) : sjbg_gs(val);
+    return sjbg_fside(val, side == 0 ? 0u : 1u);
 }
 
 __device__ __forceinline__ void flush_batch(WinAcc *acc, unsigned long long *bcount, unsigned long long count,

@@ -207,7 +207,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         if (heavy) {
             const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
             if (hid != kHeavyBucket) {
-                const unsigned long long f = right ? sjbg_gs(val) : sjbg_fr(val);
+                const unsigned long long f = sjbg_fside(val, right ? 1u : 0u);   // one mix, either side
                 atomicAdd(&hcnt[hid], 1u);
                 const uint32_t flo = (uint32_t)f;
                 const uint32_t old = atomicAdd(&hsum_lo[hid], flo);

@@ -74,6 +74,10 @@ SJBG_HD uint64_t sjbg_pair_hash(uint32_t r, uint32_t s) {
 }
 SJBG_HD uint64_t sjbg_fr(uint32_t r) { return sjbg_splitmix64((uint64_t)r << 1) | 1ull; }
 SJBG_HD uint64_t sjbg_gs(uint32_t s) { return sjbg_splitmix64(((uint64_t)s << 1) | 1ull) | 1ull; }
+/* fr (side 0) or gs (side 1) as one mix: the side is the input's low bit. */
+SJBG_HD uint64_t sjbg_fside(uint32_t v, uint32_t side) {
+    return sjbg_splitmix64(((uint64_t)v << 1) | (uint64_t)(side & 1u)) | 1ull;
+}
 
 /* ---- seeded bijection on [0, domain) --------------------------------------
  * Balanced Feistel network on 2h bits (2h >= log2(domain), h >= 1), 4 rounds,
