@@ -373,14 +373,19 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     const uint32_t nh = n_heavy_s;
     for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) M.heavy_keys[h] = ~(uint32_t)sc[h];
     SJBG_BARRIER();
-    heavy_set_build(M.heavy_set, M.heavy_keys, nh);   // ends with a barrier
+    // the set's claim scratch is the histogram's space, free until the histogram is loaded
+    static_assert(2u << kHeavyBucketsLog2 <= kBins, "claim scratch fits the histogram's space");
+    heavy_set_build(M.heavy_set, M.heavy_keys, nh, fit_smem);   // ends with a barrier
+    __shared__ uint8_t placed_s[kMaxHeavy];   // keys that found no slot stay light
+    for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x) placed_s[h] = heavy_placed(M.heavy_keys, h, fit_smem) ? 1 : 0;
+    SJBG_BARRIER();
 
     // ---- the window's light histogram, in shared memory from here on
     uint32_t *hb = fit_smem;   // kBins counters, later the inclusive CDF counts
     for (uint32_t i = threadIdx.x; i < kBins; i += blockDim.x) hb[i] = hw[i];
     SJBG_BARRIER();
     for (uint32_t h = threadIdx.x; h < nh; h += blockDim.x)
-        atomicSub(&hb[bin_of(key_x(M.heavy_keys[h], kmin, inv))], (uint32_t)(sc[h] >> 32));
+        if (placed_s[h]) atomicSub(&hb[bin_of(key_x(M.heavy_keys[h], kmin, inv))], (uint32_t)(sc[h] >> 32));
     SJBG_BARRIER();
 
     // ---- inclusive scan: warp w owns bins [w * per, (w + 1) * per), 32 at a time

@@ -22,13 +22,19 @@ namespace sjbg {
 constexpr uint32_t kMaxLeaves = 256;
 constexpr uint32_t kMaxHeavy = 512;
 constexpr uint32_t kHeavySlotsLog2 = 12;
-constexpr uint32_t kHeavySlots = 1u << kHeavySlotsLog2;   // shared-memory heavy-key table (load <= 1/8)
+constexpr uint32_t kHeavySlots = 1u << kHeavySlotsLog2;   // shared-memory heavy-key table
+constexpr uint32_t kHeavyBucketsLog2 = kHeavySlotsLog2 - 1;   // buckets of two slots (16 bytes)
 constexpr uint32_t kHeavyBucket = 0xFFFFFFFFu;            // classify(): heavy key marker
 constexpr unsigned long long kHeavyEmpty = ~0ull;
 
-// Shared-memory heavy-key set: slot = key << 32 | index, all ones when empty
-// (a heavy index is < kMaxHeavy, so no entry is all ones).  One 64-bit load
-// per probe.
+// Shared-memory heavy-key set: 2,048 buckets of two slots, slot = key << 32 |
+// index, all ones when empty (a heavy index is < kMaxHeavy, so no entry is
+// all ones).  A key lives in one of the two slots of its bucket or not at all,
+// so a lookup is one 128-bit load and two compares, with no loop: the per-tuple
+// code stays free of branches.  A key that finds its bucket full (the two
+// heavier keys of the bucket keep it; about 1% of 512 keys) is not a heavy key:
+// every kernel classifies it as light, so its tuples are joined through the
+// buckets like any light key.
 struct __align__(16) HeavySet {   // 16-byte aligned: copied with 128-bit loads and stores
     unsigned long long slot[kHeavySlots];
 };
@@ -70,22 +76,36 @@ __device__ __forceinline__ uint32_t learned_bucket(const LearnedCore &m, uint32_
     return b < P ? b : P - 1;
 }
 
-__device__ __forceinline__ uint32_t heavy_slot(uint32_t key) { return slot_hash(key, kHeavySlotsLog2); }
+__device__ __forceinline__ uint32_t heavy_bucket_of(uint32_t key) { return slot_hash(key, kHeavyBucketsLog2); }
 
-// Build a heavy-key set from keys[0..n) (one CTA; ends with a barrier).
-__device__ __forceinline__ void heavy_set_build(HeavySet &hs, const uint32_t *keys, uint32_t n) {
-    for (uint32_t i = threadIdx.x; i < kHeavySlots; i += blockDim.x) hs.slot[i] = kHeavyEmpty;
+// Build a heavy-key set from keys[0..n) (sorted heaviest first; one CTA; ends
+// with a barrier).  claim: 2 * 2^kHeavyBucketsLog2 words of shared scratch.
+// Each bucket's first slot goes to its smallest key index, the second to the
+// next smallest: the same set whatever the order the threads run in.
+__device__ __forceinline__ void heavy_set_build(HeavySet &hs, const uint32_t *keys, uint32_t n, uint32_t *claim) {
+    constexpr uint32_t nb = 1u << kHeavyBucketsLog2;
+    uint32_t *first = claim, *second = claim + nb;
+    for (uint32_t i = threadIdx.x; i < 2 * nb; i += blockDim.x) claim[i] = 0xFFFFFFFFu;
+    SJBG_BARRIER();
+    for (uint32_t h = threadIdx.x; h < n; h += blockDim.x) atomicMin(&first[heavy_bucket_of(keys[h])], h);
     SJBG_BARRIER();
     for (uint32_t h = threadIdx.x; h < n; h += blockDim.x) {
-        const uint32_t key = keys[h];
-        const unsigned long long e = ((unsigned long long)key << 32) | h;
-        uint32_t s = heavy_slot(key);
-        for (uint32_t p = 0; p < kHeavySlots; p++) {
-            if (atomicCAS(&hs.slot[s], kHeavyEmpty, e) == kHeavyEmpty) break;
-            s = (s + 1) & (kHeavySlots - 1);
-        }
+        const uint32_t b = heavy_bucket_of(keys[h]);
+        if (first[b] != h) atomicMin(&second[b], h);
     }
     SJBG_BARRIER();
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+        const uint32_t a = first[b], c = second[b];
+        hs.slot[2 * b] = a != 0xFFFFFFFFu ? (((unsigned long long)keys[a] << 32) | a) : kHeavyEmpty;
+        hs.slot[2 * b + 1] = c != 0xFFFFFFFFu ? (((unsigned long long)keys[c] << 32) | c) : kHeavyEmpty;
+    }
+    SJBG_BARRIER();
+}
+
+// Whether heavy key index h of keys[] got a slot (after heavy_set_build, with its claim scratch).
+__device__ __forceinline__ bool heavy_placed(const uint32_t *keys, uint32_t h, const uint32_t *claim) {
+    const uint32_t b = heavy_bucket_of(keys[h]);
+    return claim[b] == h || claim[(1u << kHeavyBucketsLog2) + b] == h;
 }
 
 // Copy `bytes` (a multiple of 16) from global to shared memory (all threads; ends with a barrier).
@@ -102,20 +122,12 @@ __device__ __forceinline__ void heavy_set_load(HeavySet &hs, const LearnedModel 
 }
 
 // Index of `key` among the heavy keys, or kHeavyBucket when it is light.
-// At load <= 1/8 the first slot decides almost always, so it is read without
-// a loop; only a collision walks on.
+// An empty slot reads as key 0xFFFFFFFF with index kHeavyBucket, so it needs
+// no test of its own (a bucket fills its first slot first).
 __device__ __forceinline__ uint32_t heavy_find(const HeavySet &hs, uint32_t key) {
-    uint32_t s = heavy_slot(key);
-    unsigned long long v = hs.slot[s];
-    if (v == kHeavyEmpty) return kHeavyBucket;
-    if ((uint32_t)(v >> 32) == key) return (uint32_t)v;
-    for (uint32_t p = 1; p < kHeavySlots; p++) {
-        s = (s + 1) & (kHeavySlots - 1);
-        v = hs.slot[s];
-        if (v == kHeavyEmpty) return kHeavyBucket;
-        if ((uint32_t)(v >> 32) == key) return (uint32_t)v;
-    }
-    return kHeavyBucket;
+    const uint4 b = reinterpret_cast<const uint4 *>(hs.slot)[heavy_bucket_of(key)];
+    // little-endian slots: .x index and .y key of the first, .z and .w of the second
+    return b.y == key ? b.x : (b.w == key ? b.z : kHeavyBucket);
 }
 
 }  // namespace sjbg
