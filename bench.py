@@ -558,6 +558,17 @@ def main():
         learned.lazy_execute_batch_raw(hL.data_ptr(), hR.data_ptr(), descs, e2e_res, mem=sjbg.MEM_HOST)
     e2e_s = (time.perf_counter() - t0) / ksteps
     e2e_same = [(r.count, r.prod_checksum) for r in e2e_res] == [(a[0], a[1]) for a in res_learned]
+    # the host link the end-to-end number is bound by: one plain pinned -> device
+    # copy of the left stream, event-timed (the step copies both streams)
+    link = torch.empty_like(hL, device="cuda")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    link.copy_(hL, non_blocking=True)
+    ev0.record()
+    link.copy_(hL, non_blocking=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    h2d_gbs = hL.numel() / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
+    del link
 
     tuples = 2 * total * world
     out = {
@@ -581,7 +592,8 @@ def main():
         "outputs_identical_learned_vs_plain": same,   # and vs radix (learned fan-out) and the HBM table
         "latency": {"p50_ms": p50, "p99_ms": p99, "windows": len(lat), "unit": "ms per window call"},
         "e2e": {"value": tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": 32 * total,
-                "d2h_bytes_per_step": 32 * nwin, "outputs_identical": e2e_same},
+                "d2h_bytes_per_step": 32 * nwin, "outputs_identical": e2e_same,
+                "h2d_link_gbs": h2d_gbs, "link_bound_tuples_per_s": h2d_gbs * 1e9 / 16},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
