@@ -17,11 +17,11 @@
 //                    is written as contiguous per-bucket runs of (key,val) words.
 //   4. bucket_join   one CTA per (window, bucket): build an open-addressing table
 //                    in shared memory from the left run, probe with the right run.
-//        count mode: table slot = {key, count, sum fr(val)}; duplicates inside a
-//                    warp are pre-aggregated with __match_any_sync so a hot key
-//                    costs one shared atomic per warp; keys that do not fit go
-//                    back into the left run (compacted in place) and are joined
-//                    in a further pass, so any bucket, however skewed, finishes.
+//        count mode: table slot = {key, count, sum fr(val)}, updated with
+//                    32-bit shared atomics (the sum as two words with carry);
+//                    keys that do not fit go back into the left run (compacted
+//                    in place) and are joined in a further pass, so any bucket,
+//                    however skewed, finishes.
 //        enum mode:  table slot = {key, chain head}, chains over a staged chunk
 //                    of left vals; every pair is visited for the xor checksum
 //                    and, when asked, written with one atomic per warp.
@@ -848,14 +848,27 @@ __device__ __forceinline__ uint32_t ct_home(uint32_t key, uint32_t C) {
     return (uint32_t)(((uint64_t)slot_hash(key, 32) * C) >> 32);
 }
 
+// Adds f to a table slot's fr-sum as two 32-bit words (native shared atomics;
+// the low word's carry, seen in its returned old value, goes to the high word).
+// A 64-bit shared atomicAdd is a compare-and-swap loop, which hot keys turn
+// into a long serial chain.
+__device__ __forceinline__ void ct_add_sum(unsigned long long *slot, unsigned long long f) {
+    uint32_t *w2 = reinterpret_cast<uint32_t *>(slot);   // little-endian: low word first
+    const uint32_t flo = (uint32_t)f;
+    const uint32_t old = atomicAdd(&w2[0], flo);
+    atomicAdd(&w2[1], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
+}
+
 // Insert `c` tuples of `key` with fr-sum `f`.  A key that finds neither itself
 // nor a free slot within kMaxProbe slots is refused (false) and joined in a
 // later pass; lookups use the same bound, so a refused key is never half-found.
+// Every lane inserts its own tuple: with the sums' native 32-bit atomics this
+// beats combining a warp's equal keys first, at every skew measured.
 __device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uint32_t c, unsigned long long f) {
     const uint32_t C = t.C;
     if (key == kEmptyKey) {
         atomicAdd(&t.cnt[C], c);
-        atomicAdd(&t.sumf[C], f);
+        ct_add_sum(&t.sumf[C], f);
         return true;
     }
     uint32_t s = ct_home(key, C);
@@ -867,7 +880,7 @@ __device__ __forceinline__ bool ct_insert(const CountTable &t, uint32_t key, uin
         }
         if (k == key) {
             atomicAdd(&t.cnt[s], c);
-            atomicAdd(&t.sumf[s], f);
+            ct_add_sum(&t.sumf[s], f);
             return true;
         }
         s = s + 1 == C ? 0 : s + 1;
@@ -886,31 +899,6 @@ __device__ __forceinline__ int ct_lookup(const CountTable &t, uint32_t key) {
         s = s + 1 == C ? 0 : s + 1;
     }
     return -1;
-}
-
-// Warp-aggregated insert: lanes holding the same key combine (count, fr-sum)
-// and only the group leader touches the table; every member follows its
-// leader's outcome.  All 32 lanes must call it.
-__device__ __forceinline__ bool agg_insert(const CountTable &t, bool valid, uint32_t key, unsigned long long f) {
-    const unsigned full = 0xFFFFFFFFu;
-    const uint32_t lane = lane_id();
-    const unsigned active = __ballot_sync(full, valid);
-    unsigned grp = __match_any_sync(full, key) & active;
-    if (!valid) grp = 1u << lane;
-    const int leader = __ffs(grp) - 1;
-    const uint32_t gsize = __popc(grp);
-    unsigned long long gsum = f;
-    unsigned multi = __ballot_sync(full, valid && gsize > 1 && (int)lane == leader);
-    while (multi) {
-        const int ld = __ffs(multi) - 1;
-        multi &= multi - 1;
-        const unsigned m = __shfl_sync(full, grp, ld);
-        const unsigned long long sm = warp_sum_u64(((m >> lane) & 1u) ? f : 0ull);
-        if ((int)lane == ld) gsum = sm;
-    }
-    bool ok = true;
-    if (valid && (int)lane == leader) ok = ct_insert(t, key, gsize, gsum);
-    return __shfl_sync(full, ok, leader);
 }
 
 constexpr int kJoinPer = 8;   // elements per thread per tile (independent loads in flight)
@@ -960,7 +948,7 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
             for (int k = 0; k < kJoinPer; k++) {
                 const uint32_t i = base + k * blockDim.x + threadIdx.x;
                 const bool valid = i < n;
-                const bool ok = agg_insert(t, valid, (uint32_t)e[k], valid ? sjbg_fr((uint32_t)(e[k] >> 32)) : 0ull);
+                const bool ok = !valid || ct_insert(t, (uint32_t)e[k], 1u, sjbg_fr((uint32_t)(e[k] >> 32)));
                 if (valid && !ok) Rb[atomicAdd(&novf, 1u)] = e[k];
             }
         }
