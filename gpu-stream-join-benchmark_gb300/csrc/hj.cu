@@ -53,6 +53,8 @@ __host__ __device__ __forceinline__ uint32_t coarse_bits(uint32_t lg) { return (
 // Windows of at least this many buckets are partitioned in two passes: with
 // fewer, a 4,096-tuple tile still writes runs of several tuples per bucket.
 constexpr uint32_t kTwoLevelMinLog2 = 11;
+// Heavy keys whose counting-pass accumulators are replicated per lane.
+constexpr uint32_t kHotHeavy = 32;
 
 __device__ __forceinline__ uint32_t find_window(const uint32_t *prefix, uint32_t n, uint32_t t) {
     // largest w with prefix[w] <= t  (prefix has n+1 entries, prefix[0] = 0)
@@ -130,8 +132,13 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     extern __shared__ __align__(16) uint32_t hist[];   // P counters, then (coarse output) the tile stage
     __shared__ HeavySet hs;
     // heavy-key sums as two 32-bit words: native 32-bit shared atomics, with
-    // the low word's carry (seen in its returned old value) added to the high word
-    __shared__ uint32_t hcnt[kMaxHeavy], hsum_lo[kMaxHeavy], hsum_hi[kMaxHeavy];
+    // the low word's carry (seen in its returned old value) added to the high
+    // word.  The kHotHeavy heaviest keys (ids 0 .. kHotHeavy-1, heaviest first)
+    // have one copy per lane after the kMaxHeavy shared ones: copy kMaxHeavy +
+    // 32 * id + lane sits in the lane's own bank, so the many lanes of a warp
+    // that hold the same hot key update it without bank conflicts.
+    constexpr uint32_t kHeavySlotsAcc = kMaxHeavy + 32 * kHotHeavy;
+    __shared__ uint32_t hcnt[kHeavySlotsAcc], hsum_lo[kHeavySlotsAcc], hsum_hi[kHeavySlotsAcc];
     __shared__ uint32_t cwarp[2][32], cbase[2];   // light-tuple compaction, double-buffered by tile
     // this CTA covers tiles [t, t + kHistTiles) of one window side ("hist groups")
     const bool right = blockIdx.x >= hgroupL[nwin];
@@ -165,7 +172,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     const uint32_t P = 1u << (cls.m ? cls.m->log2_buckets : wp.log2_buckets);
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
     if (heavy) {
-        for (uint32_t i = threadIdx.x; i < kMaxHeavy; i += blockDim.x) { hcnt[i] = 0; hsum_lo[i] = 0; hsum_hi[i] = 0; }
+        for (uint32_t i = threadIdx.x; i < kHeavySlotsAcc; i += blockDim.x) { hcnt[i] = 0; hsum_lo[i] = 0; hsum_hi[i] = 0; }
         heavy_set_load(hs, gm);   // ends with a barrier
     }
     SJBG_BARRIER();
@@ -208,10 +215,11 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
             if (hid != kHeavyBucket) {
                 const unsigned long long f = sjbg_fside(val, right ? 1u : 0u);   // one mix, either side
-                atomicAdd(&hcnt[hid], 1u);
+                const uint32_t a = hid < kHotHeavy ? kMaxHeavy + 32u * hid + lane_id() : hid;
+                atomicAdd(&hcnt[a], 1u);
                 const uint32_t flo = (uint32_t)f;
-                const uint32_t old = atomicAdd(&hsum_lo[hid], flo);
-                atomicAdd(&hsum_hi[hid], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
+                const uint32_t old = atomicAdd(&hsum_lo[a], flo);
+                atomicAdd(&hsum_hi[a], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
             } else if (valid) {
                 // light keys: compacted windows count them in part_hist_light
                 if (compact) {
@@ -299,6 +307,21 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
         if (hist[i]) atomicAdd(&dst[i], hist[i]);
     if (heavy) {
+        // fold the hot keys' per-lane copies into their shared slots: warp q sums key q's
+        for (uint32_t q = warp_id(); q < kHotHeavy; q += blockDim.x >> 5) {
+            const uint32_t a = kMaxHeavy + 32u * q + lane_id();
+            uint32_t c = hcnt[a];
+            unsigned long long sm = ((unsigned long long)hsum_hi[a] << 32) | hsum_lo[a];
+            sm = warp_sum_u64(sm);
+            for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+            if (lane_id() == 0) {
+                // slot q itself is never updated by the counting loop
+                hcnt[q] = c;
+                hsum_lo[q] = (uint32_t)sm;
+                hsum_hi[q] = (uint32_t)(sm >> 32);
+            }
+        }
+        SJBG_BARRIER();
         HeavyAcc *ha = hacc + (uint64_t)w * kMaxHeavy;
         for (uint32_t i = threadIdx.x; i < cls.m->n_heavy; i += blockDim.x) {
             if (!hcnt[i]) continue;
