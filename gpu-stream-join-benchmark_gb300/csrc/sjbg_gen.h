@@ -68,15 +68,31 @@ SJBG_HD uint32_t sjbg_uniform_key(uint64_t seed, uint64_t i, uint64_t domain) {
  * prod checksum = sum over matching pairs of sjbg_fr(r) * sjbg_gs(s) mod 2^64
  *               = sum over keys k of (sum_{r in R_k} fr(r)) * (sum_{s in S_k} gs(s)),
  *   which is still a function of the exact pair multiset but costs O(|R|+|S|).
- * r and s are the val fields of the left (R) and right (S) tuples. */
+ * r and s are the val fields of the left (R) and right (S) tuples.
+ *
+ * fr and gs are computed once per tuple in the hash join's hot loops, so they
+ * use a two-multiply mixer of 32-bit words instead of the 64-bit SplitMix64
+ * finaliser: h1 = (x ^ k) * A (32x32 -> 64 bits; its low half is a bijection
+ * of x), h2 = (lo(h1) ^ hi(h1) ^ c) * B, result = h1 ^ (h2 << 32) ^ (h2 >> 13),
+ * forced odd.  A = 0x9E3779B1 and B = 0x85EBCA77 are the odd 32-bit
+ * multipliers of Knuth's multiplicative hashing and of MurmurHash3's
+ * finaliser; the side keys k (0x243F6A88 left, 0xB7E15162 right) are the
+ * leading hex digits of pi and e.  The xor checksum keeps SplitMix64. */
 SJBG_HD uint64_t sjbg_pair_hash(uint32_t r, uint32_t s) {
     return sjbg_splitmix64(((uint64_t)r << 32) | (uint64_t)s);
 }
-SJBG_HD uint64_t sjbg_fr(uint32_t r) { return sjbg_splitmix64((uint64_t)r << 1) | 1ull; }
-SJBG_HD uint64_t sjbg_gs(uint32_t s) { return sjbg_splitmix64(((uint64_t)s << 1) | 1ull) | 1ull; }
-/* fr (side 0) or gs (side 1) as one mix: the side is the input's low bit. */
+#define SJBG_FR_KEY 0x243F6A88u
+#define SJBG_GS_KEY 0xB7E15162u
+SJBG_HD uint64_t sjbg_mix32(uint32_t x, uint32_t k) {
+    const uint64_t h1 = (uint64_t)(x ^ k) * 0x9E3779B1u;
+    const uint64_t h2 = (uint64_t)((uint32_t)h1 ^ (uint32_t)(h1 >> 32) ^ 0x7F4A7C15u) * 0x85EBCA77u;
+    return h1 ^ (h2 << 32) ^ (h2 >> 13);
+}
+SJBG_HD uint64_t sjbg_fr(uint32_t r) { return sjbg_mix32(r, SJBG_FR_KEY) | 1ull; }
+SJBG_HD uint64_t sjbg_gs(uint32_t s) { return sjbg_mix32(s, SJBG_GS_KEY) | 1ull; }
+/* fr (side 0) or gs (side 1), the side chosen by the key alone. */
 SJBG_HD uint64_t sjbg_fside(uint32_t v, uint32_t side) {
-    return sjbg_splitmix64(((uint64_t)v << 1) | (uint64_t)(side & 1u)) | 1ull;
+    return sjbg_mix32(v, side ? SJBG_GS_KEY : SJBG_FR_KEY) | 1ull;
 }
 
 /* ---- seeded bijection on [0, domain) --------------------------------------
