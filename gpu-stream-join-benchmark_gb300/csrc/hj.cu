@@ -139,7 +139,6 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     // that hold the same hot key update it without bank conflicts.
     constexpr uint32_t kHeavySlotsAcc = kMaxHeavy + 32 * kHotHeavy;
     __shared__ uint32_t hcnt[kHeavySlotsAcc], hsum_lo[kHeavySlotsAcc], hsum_hi[kHeavySlotsAcc];
-    __shared__ uint32_t cwarp[2][32], cbase[2];   // light-tuple compaction, double-buffered by tile
     // this CTA covers tiles [t, t + kHistTiles) of one window side ("hist groups")
     const bool right = blockIdx.x >= hgroupL[nwin];
     const uint32_t g = right ? blockIdx.x - hgroupL[nwin] : blockIdx.x;
@@ -192,6 +191,20 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             const uint32_t i = threadIdx.x + k * kPartThreads;
             v[k] = i < n ? __ldg(src + 2 * i) : make_uint2(0u, 0u);
         }
+    };
+    // compacted windows: each warp buffers its light tuples in its share of the
+    // stage (which only coarse output uses otherwise); wn is warp-uniform
+    constexpr uint32_t kWarpBuf = kTile / (kPartThreads / 32);   // a warp's tile fits an empty buffer
+    uint64_t *wbuf = stage + warp_id() * kWarpBuf;
+    uint32_t wn = 0;
+    auto flush_light = [&]() {
+        uint32_t base = 0;
+        if (lane_id() == 0) base = atomicAdd(&ccnt[2 * w + (right ? 1 : 0)], wn);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        __syncwarp();   // the buffer's writes are visible to every lane
+        for (uint32_t j = lane_id(); j < wn; j += 32) cdst[base + j] = wbuf[j];
+        __syncwarp();   // read before it is refilled
+        wn = 0;
     };
     // software pipeline: tile tt+1 is in flight while tile tt is counted
     uint2 nv[kPer];
@@ -280,28 +293,21 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) dst[i] = stage[i];
     }
     if (compact) {
-        // the tile's light tuples go to the window side's compact array as
-        // (key,val) words: warp scan, block scan, one global reservation
-        const uint32_t par = tt & 1u;
+        // the tile's light tuples go to the warp's buffer as (key,val) words
+        // (warp scan, no block barrier); a full buffer is written out to the
+        // window side's compact array with one global reservation
         const uint32_t nl = __popc(lightmask);
         uint32_t wt;
         const uint32_t ex = warp_excl_scan(nl, &wt);
-        if (lane_id() == 31) cwarp[par][warp_id()] = ex + nl;
-        SJBG_BARRIER();
-        if (warp_id() == 0) {
-            const uint32_t x = lane_id() < (blockDim.x >> 5) ? cwarp[par][lane_id()] : 0u;
-            uint32_t tot;
-            const uint32_t e = warp_excl_scan(x, &tot);
-            cwarp[par][lane_id()] = e;
-            if (lane_id() == 0) cbase[par] = tot ? atomicAdd(&ccnt[2 * w + (right ? 1 : 0)], tot) : 0u;
-        }
-        SJBG_BARRIER();
-        uint32_t pos = cbase[par] + cwarp[par][warp_id()] + ex;
+        if (wn + wt > kWarpBuf) flush_light();
+        uint32_t pos = wn + ex;
 #pragma unroll
         for (int k = 0; k < kPer; k++)
-            if ((lightmask >> k) & 1u) cdst[pos++] = ((uint64_t)v[k].y << 32) | v[k].x;
+            if ((lightmask >> k) & 1u) wbuf[pos++] = ((uint64_t)v[k].y << 32) | v[k].x;
+        wn += wt;
     }
     }
+    if (compact && wn) flush_light();
     SJBG_BARRIER();
     uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
