@@ -44,6 +44,7 @@ WORKLOADS = {
     "uniform_hj_16x65536": (16, 65536, 65536, None),
     # reduced case of the skewed workload for profiler captures (inputs still > L2)
     "skewed_hj_small": (2, 1 << 22, 1 << 24, 1.5),
+    "skewed_hj_small_z1.0": (2, 1 << 22, 1 << 24, 1.0),
 }
 
 

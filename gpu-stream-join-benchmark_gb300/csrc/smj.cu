@@ -169,7 +169,7 @@ int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
         lens[n + w] = wins[w].n_right;
         srcs[n + w] = wins[w].right_off;
     }
-    const SortPlan plan = sort_plan(lens.data(), srcs.data(), 2 * n);
+    SortPlan plan = sort_plan(lens.data(), srcs.data(), 2 * n);
     std::vector<MergeWin> mw(n);
     uint32_t cuts = 0, tiles = 0;
     for (uint32_t w = 0; w < n; w++) {
@@ -203,6 +203,7 @@ int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
     if (int rc_up = stage_copy(h, dev, hst, segB + mwB)) return rc_up;
     const SortSeg *dSegs = reinterpret_cast<const SortSeg *>(dev);
     const MergeWin *dMw = reinterpret_cast<const MergeWin *>(dev + segB);
+    if (int rc_map = sort_tile_map(h, plan, dSegs)) return rc_map;
 
     int rc = sort_extract(h, dL, dR, n, plan, dSegs, k0, v0);
     if (!rc) rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1, reinterpret_cast<uint32_t *>(&acc[n].info));

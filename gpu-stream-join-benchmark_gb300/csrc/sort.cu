@@ -9,8 +9,10 @@
 //   rs_downsweep  per tile: the tile's keys and vals are staged in shared
 //                 memory by TMA bulk copies (cp.async.bulk, mbarrier with a
 //                 bounded wait); stable ranks come from warp-private digit
-//                 counters and __match_any_sync; the tile is reordered in
-//                 shared memory and written as contiguous per-digit runs.
+//                 counters and each lane's digit peers (nine ballots: faster
+//                 than __match_any_sync); the tile is reordered in shared
+//                 memory and written as contiguous per-digit runs.
+// Every per-tile kernel finds its segment in the plan's tile map (one load).
 // The reference's GPU sort-merge join uses a counting sort by key with
 // unstable atomics instead (src/sjb/windowing/lazy/executor/GPU/GPU_SMJ.cu:19-32).
 #include <algorithm>
@@ -80,12 +82,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // ------------------------------------------------------------------ kernels
+// Lanes of the warp holding the same 9-bit digit (256 = no element): one
+// ballot per bit, each lane keeping the lanes that agree with it on that bit.
+__device__ __forceinline__ unsigned digit_peers(uint32_t d) {
+    unsigned peers = 0xFFFFFFFFu;
+#pragma unroll
+    for (int b = 0; b < 9; b++) {
+        const bool bit = (d >> b) & 1u;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
+
 // Segments [0, split) read srcA, the others srcB.
 __global__ void __launch_bounds__(256)
 sort_extract_kernel(const sjbg_tuple *__restrict__ srcA, const sjbg_tuple *__restrict__ srcB, uint32_t split,
-                    const SortSeg *__restrict__ segs, uint32_t nseg, uint32_t *__restrict__ keys,
+                    const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t *__restrict__ keys,
                     uint32_t *__restrict__ vals) {
-    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const sjbg_tuple *src = s < split ? srcA : srcB;
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
@@ -103,9 +118,9 @@ sort_extract_kernel(const sjbg_tuple *__restrict__ srcA, const sjbg_tuple *__res
 }
 
 __global__ void __launch_bounds__(256)
-sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, uint32_t nseg,
+sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg,
                 uint32_t *__restrict__ out) {
-    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
     uint32_t m = 0;
@@ -117,10 +132,10 @@ sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ s
 
 // counts block of segment s: counts[tile0 * 256 + d * ntiles + t_local]
 __global__ void __launch_bounds__(256)
-rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, uint32_t nseg, uint32_t shift,
+rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t shift,
                   uint32_t *__restrict__ counts) {
     __shared__ uint32_t hist[kDigits];
-    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t tl = blockIdx.x - sg.tile0;
     const uint32_t base = tl * kSortTile;
@@ -140,7 +155,7 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
             const bool valid = e0 + c < sg.n;
             const uint32_t d = valid ? (kk[c] >> shift) & 0xFFu : 0u;
             // skewed keys share digits: combine equal digits of the warp first
-            const unsigned grp = __match_any_sync(0xFFFFFFFFu, valid ? d : 0x100u);
+            const unsigned grp = digit_peers(valid ? d : 0x100u);
             if (valid && lane_id() == (uint32_t)(__ffs(grp) - 1)) atomicAdd(&hist[d], (uint32_t)__popc(grp));
         }
     }
@@ -205,11 +220,11 @@ struct DownSmem {
 __global__ void __launch_bounds__(kSortThreads)
 rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
-                    const SortSeg *__restrict__ segs, uint32_t nseg, uint32_t shift,
+                    const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t shift,
                     const uint32_t *__restrict__ counts, uint32_t *__restrict__ status) {
     extern __shared__ __align__(128) uint8_t smem_raw[];
     DownSmem &sm = *reinterpret_cast<DownSmem *>(smem_raw);
-    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t tl = blockIdx.x - sg.tile0;
     const uint32_t base = tl * kSortTile;
@@ -242,7 +257,7 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
     for (int k = 0; k < kItems; k++) {
         const uint32_t pos = w * (kSortTile / kSortWarps) + k * 32 + lane;
         const uint32_t d = pos < n ? (sm.in_keys[pos] >> shift) & 0xFFu : kDigits;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned peers = digit_peers(d);
         const uint32_t cur = sm.wcnt[w][d];
         __syncwarp();
         rank[k] = cur + __popc(peers & lt_mask);
@@ -301,10 +316,10 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
 // ---- segmented exclusive prefix of fr(val): tile sums, per-segment scan of the
 // ---- tile sums, per-tile scan plus offset
 __global__ void __launch_bounds__(256)
-fr_tile_sum_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, uint32_t nseg,
+fr_tile_sum_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg,
                    unsigned long long *__restrict__ tsum) {
     __shared__ unsigned long long ws[8];
-    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
     unsigned long long acc = 0;
@@ -333,10 +348,10 @@ __global__ void fr_seg_scan_kernel(unsigned long long *__restrict__ tsum, const 
 }
 
 __global__ void __launch_bounds__(256)
-fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, uint32_t nseg,
+fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg,
                     const unsigned long long *__restrict__ tsum, unsigned long long *__restrict__ out) {
     __shared__ unsigned long long wsum[8];
-    const uint32_t s = find_seg(segs, nseg, blockIdx.x);
+    const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
     constexpr uint32_t kPer = kSortTile / 256;   // 16 consecutive elements per thread
@@ -362,11 +377,26 @@ fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict
     }
 }
 
+__global__ void __launch_bounds__(256) sort_tile_map_kernel(const SortSeg *__restrict__ segs, uint32_t *__restrict__ map) {
+    const SortSeg sg = segs[blockIdx.x];
+    for (uint32_t t = threadIdx.x; t < sg.ntiles; t += blockDim.x) map[sg.tile0 + t] = blockIdx.x;
+}
+
 // ------------------------------------------------------------------ host drivers
+int sort_tile_map(sjbg_handle *h, SortPlan &plan, const SortSeg *dSegs) {
+    uint32_t *map = static_cast<uint32_t *>(ws_get(h, WS_SORT_MAP, sizeof(uint32_t) * std::max(plan.tiles, 1u)));
+    if (!map) return fail(h, SJBG_E_NOMEM, "sort tile map");
+    if (!plan.segs.empty())
+        SJBG_CK(h, launch(h, "sort_tile_map", sort_tile_map_kernel, dim3((uint32_t)plan.segs.size()), dim3(256), 0,
+                          dSegs, map));
+    plan.tile_seg = map;
+    return SJBG_OK;
+}
+
 int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB, uint32_t split, const SortPlan &plan,
                  const SortSeg *dSegs, uint32_t *keys, uint32_t *vals) {
     SJBG_CK(h, launch(h, "sort_extract", sort_extract_kernel, dim3(plan.tiles), dim3(256), 0, srcA, srcB, split, dSegs,
-                      (uint32_t)plan.segs.size(), keys, vals));
+                      plan.tile_seg, keys, vals));
     return SJBG_OK;
 }
 
@@ -381,7 +411,7 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
     if (!h->capturing) {
         SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
         SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys,
-                          dSegs, nseg, dMax));
+                          dSegs, plan.tile_seg, dMax));
         SJBG_CK(h, cudaMemcpyAsync(hMax, dMax, 8, cudaMemcpyDeviceToHost, h->stream));
         SJBG_CK(h, cudaStreamSynchronize(h->stream));
         maxk = hMax[0];
@@ -395,10 +425,10 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
     for (uint32_t p = 0; p < passes; p++) {
         const uint32_t shift = 8 * p;
         SJBG_CK(h, launch(h, "rs_upsweep", rs_upsweep_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)kin,
-                          dSegs, nseg, shift, counts));
+                          dSegs, plan.tile_seg, shift, counts));
         SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs));
         SJBG_CK(h, launch(h, "rs_downsweep", rs_downsweep_kernel, dim3(plan.tiles), dim3(kSortThreads), smem,
-                          (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, nseg, shift,
+                          (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, plan.tile_seg, shift,
                           (const uint32_t *)counts, status));
         std::swap(kin, kout);
         std::swap(vin, vout);
@@ -417,9 +447,9 @@ int segmented_fr_prefix(sjbg_handle *h, const SortPlan &plan, uint32_t nseg, con
     const uint32_t tiles = nseg < plan.segs.size() ? plan.segs[nseg].tile0 : plan.tiles;
     unsigned long long *tsum = static_cast<unsigned long long *>(ws_get(h, WS_AUX3, sizeof(unsigned long long) * tiles));
     if (!tsum) return fail(h, SJBG_E_NOMEM, "prefix buffers");
-    SJBG_CK(h, launch(h, "fr_tile_sum", fr_tile_sum_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, nseg, tsum));
+    SJBG_CK(h, launch(h, "fr_tile_sum", fr_tile_sum_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, plan.tile_seg, tsum));
     SJBG_CK(h, launch(h, "fr_seg_scan", fr_seg_scan_kernel, dim3(nseg), dim3(32), 0, tsum, dSegs));
-    SJBG_CK(h, launch(h, "fr_tile_scan", fr_tile_scan_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, nseg,
+    SJBG_CK(h, launch(h, "fr_tile_scan", fr_tile_scan_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, plan.tile_seg,
                       (const unsigned long long *)tsum, out));
     return SJBG_OK;
 }

@@ -26,6 +26,7 @@ struct SortPlan {
     std::vector<SortSeg> segs;
     uint32_t tiles = 0;
     uint64_t elems = 0;   // padded total
+    const uint32_t *tile_seg = nullptr;   // device: segment of every tile (sort_tile_map)
 };
 
 // Plan segments of lengths n[0..k) read from AoS offsets src[0..k): padded
@@ -37,14 +38,12 @@ SortPlan sort_plan(const uint64_t *n, const uint64_t *src, uint32_t k);
 int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB, uint32_t split, const SortPlan &plan,
                  const SortSeg *dSegs, uint32_t *keys, uint32_t *vals);
 
-__device__ __forceinline__ uint32_t find_seg(const SortSeg *segs, uint32_t nseg, uint32_t tile) {
-    uint32_t lo = 0, hi = nseg;   // largest s with segs[s].tile0 <= tile
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (segs[mid].tile0 <= tile) lo = mid; else hi = mid;
-    }
-    return lo;
-}
+// Writes the segment of every tile of the plan into a workspace array (one
+// launch) and points plan.tile_seg at it: the per-tile kernels then find
+// their segment with one load instead of a binary search over the segments.
+int sort_tile_map(sjbg_handle *h, SortPlan &plan, const SortSeg *dSegs);
+
+__device__ __forceinline__ uint32_t find_seg(const uint32_t *tile_seg, uint32_t tile) { return tile_seg[tile]; }
 
 // Stable LSD sort of every segment by key; keys/vals hold the input and the
 // sorted result on return (keys2/vals2 are scratch).  Passes = ceil(bits/8)
