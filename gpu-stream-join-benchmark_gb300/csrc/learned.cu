@@ -524,7 +524,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
                 lo = prev;
                 hi = fmaxf(lfit[l][4], lo);
             }
-            M.slope[l] = slope; M.mean_x[l] = mx; M.mean_y[l] = my; M.lo[l] = lo; M.hi[l] = hi;
+            M.leaf[l] = make_float4(slope, my - slope * mx, lo, hi);
             prev = hi;
         }
         if (lane == 0) {

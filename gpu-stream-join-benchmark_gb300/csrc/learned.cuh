@@ -4,7 +4,9 @@
 // piecewise-linear approximation of the CDF of its light (non-heavy) keys:
 //   x      = clamp((key - kmin) * inv_range, 0, 1)                (FP32)
 //   leaf   = clamp(floor((root_a * x + root_b) * leaves), 0, leaves-1)
-//   cdf    = clamp(mean_y[leaf] + slope[leaf] * (x - mean_x[leaf]), lo[leaf], hi[leaf])
+//   cdf    = clamp(slope[leaf] * x + icpt[leaf], lo[leaf], hi[leaf])
+//            (the leaf's least-squares line, fitted around its centroid,
+//            stored as slope and intercept: one 128-bit load per lookup)
 //   bucket = min(P - 1, floor(cdf * P))
 // lo/hi are the smallest/largest sampled CDF values routed to the leaf, made
 // non-decreasing across leaves, which keeps the whole map monotone in key.
@@ -46,7 +48,7 @@ struct __align__(16) LearnedCore {
     uint32_t leaves, log2_buckets, fallback, n_heavy;
     uint32_t compact;     // light tuples are compacted while counting (most tuples are heavy)
     uint32_t pad_[3];
-    float slope[kMaxLeaves], mean_x[kMaxLeaves], mean_y[kMaxLeaves], lo[kMaxLeaves], hi[kMaxLeaves];
+    float4 leaf[kMaxLeaves];   // per leaf {slope, intercept, lo, hi}
 };
 
 struct LearnedModel : LearnedCore {
@@ -70,8 +72,9 @@ __device__ __forceinline__ uint32_t learned_bucket(const LearnedCore &m, uint32_
     x = fminf(fmaxf(x, 0.0f), 1.0f);
     int leaf = (int)floorf((m.root_a * x + m.root_b) * (float)m.leaves);
     leaf = min(max(leaf, 0), (int)m.leaves - 1);
-    float y = m.mean_y[leaf] + m.slope[leaf] * (x - m.mean_x[leaf]);
-    y = fminf(fmaxf(y, m.lo[leaf]), m.hi[leaf]);
+    const float4 lf = m.leaf[leaf];
+    float y = fmaf(lf.x, x, lf.y);
+    y = fminf(fmaxf(y, lf.z), lf.w);
     uint32_t b = (uint32_t)(y * (float)P);
     return b < P ? b : P - 1;
 }
