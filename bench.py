@@ -45,6 +45,8 @@ WORKLOADS = {
     # reduced case of the skewed workload for profiler captures (inputs still > L2)
     "skewed_hj_small": (2, 1 << 22, 1 << 24, 1.5),
     "skewed_hj_small_z1.0": (2, 1 << 22, 1 << 24, 1.0),
+    # two windows large enough for two-level partitioning (2^11 buckets)
+    "skewed_hj_mid_z1.0": (2, 1 << 23, 1 << 24, 1.0),
 }
 
 
@@ -223,13 +225,25 @@ def bench_batched(args, sjbg, torch, dev):
                         args.steps, args.warmup)
     ms_s = _events_time(torch, stream, lambda: smj.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res_s),
                         max(1, args.steps // 2), 2)
+    # the partitioned hash join on the same windows (what the autotuner weighs
+    # against one HBM table per window)
+    rdx = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, partitioner=sjbg.PART_RADIX, flags=sjbg.F_GRAPH,
+                      max_tuples_per_window=1 << 20, device=dev)
+    rdx.set_stream(stream.cuda_stream)
+    res_r = (sjbg.WindowResult * 1024)()
+    ms_r = _events_time(torch, stream, lambda: rdx.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res_r),
+                        max(1, args.steps // 2), 2)
     same = [(a.count, a.prod_checksum) for a in res_h] == [(a.count, a.prod_checksum) for a in res_s]
+    same_r = [(a.count, a.prod_checksum) for a in res_h] == [(a.count, a.prod_checksum) for a in res_r]
     hj.close()
     smj.close()
+    rdx.close()
     tuples = 2 * total
     return _line("joined input tuples/s", tuples / (ms_h * 1e-3), "tuples/s", ms_h, args, "batched_1024",
                  {"sort_merge": {"value": tuples / (ms_s * 1e-3), "ms_per_step": ms_s},
-                  "outputs_identical_hash_vs_sort_merge": same, "tuples_per_step": tuples,
+                  "hash_radix_partitioned": {"value": tuples / (ms_r * 1e-3), "ms_per_step": ms_r},
+                  "outputs_identical_hash_vs_sort_merge": same, "outputs_identical_hash_vs_radix": same_r,
+                  "tuples_per_step": tuples,
                   "notes": "hash join autotuned + CUDA-graph replay; sort-merge graph replay (4 radix passes)"})
 
 
