@@ -194,6 +194,70 @@ def test_learned_keeps_its_model_when_many_keys_are_hot(lib, oracle, z):
     assert (got["count"], got["prod"]) == (want["count"], want["prod"]) == (rad["count"], rad["prod"])
 
 
+def test_learned_heavy_keys_sharing_a_set_bucket(lib, oracle):
+    """The heavy-key set has 2,048 buckets of two slots (bucket = top 11 bits of
+    key * 0x9E3779B97F4A7C15).  Four heavy keys of one bucket: the two heaviest
+    take its slots, the other two find it full and stay light, and are joined
+    through the partitions; the result still equals the oracle and radix."""
+    C, M = 0x9E3779B97F4A7C15, (1 << 64) - 1
+    by_bucket = {}
+    for k in range(1, 1 << 20):
+        group = by_bucket.setdefault(((k * C) & M) >> 53, [])
+        group.append(k)
+        if len(group) == 4:
+            break
+    hot = group                                           # four keys of one bucket
+    mult = [300_000, 250_000, 6_000, 5_000]               # heaviest first
+    rng = np.random.default_rng(11)
+    sides = []
+    for side in range(2):
+        keys = np.concatenate([np.full(m, k, np.uint32) for k, m in zip(hot, mult)] +
+                              [rng.integers(1 << 24, (1 << 24) + (1 << 22), 1_000_000, dtype=np.uint32)])
+        rng.shuffle(keys)
+        sides.append(make_tuples(keys, first=side << 28))
+    left, right = sides
+    want = oracle.join(left, right, enumerate_pairs=False)
+    n = len(left)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=n) as j:
+        got = j.lazy_execute(left, right)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, max_tuples_per_window=n) as j:
+        rad = j.lazy_execute(left, right)
+    assert got["partitioner_used"] == lib.PART_LEARNED and not (got["flags"] & lib.WR_FALLBACK)
+    assert (got["count"], got["prod"]) == (want["count"], want["prod"]) == (rad["count"], rad["prod"])
+
+
+def test_learned_batch_mixes_every_kind_of_window(lib, oracle):
+    """One call whose windows take every route of the later passes, which visit
+    only the tiles and buckets listed for them: a compacted z = 1.5 window, a
+    uniform 2^23 window (two-level: coarse runs, then the fine pass), a z = 1.0
+    window, a tiny window and one with an empty side.  Each equals the oracle
+    and radix partitioning."""
+    D = 1 << 24
+    t15, t10 = oracle.zipf_table(D, 1.5), oracle.zipf_table(D, 1.0)
+    spec = [("z15", 1 << 20, 1 << 20), ("uni", 1 << 23, 1 << 23), ("z10", 1 << 21, 1 << 21),
+            ("uni", 1000, 900), ("uni", 5000, 0)]
+    lefts, rights, descs, lo, ro = [], [], [], 0, 0
+    for kind, nl, nr in spec:
+        if kind == "uni":
+            l, r = oracle.gen_uniform(lo, nl, 1, D), oracle.gen_uniform(ro, nr, 2, D)
+        else:
+            tab = t15 if kind == "z15" else t10
+            l, r = oracle.gen_zipf(lo, nl, 1, tab, D, 3), oracle.gen_zipf(ro, nr, 2, tab, D, 3)
+        lefts.append(l)
+        rights.append(r)
+        descs.append((lo, nl, ro, nr, 0, 0))
+        lo += nl
+        ro += nr
+    left, right = np.concatenate(lefts), np.concatenate(rights)
+    want, _ = oracle.join_windows(left, right, descs, enumerate_pairs=False)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=1 << 23) as j:
+        got = j.lazy_execute_batch(left, right, descs)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, max_tuples_per_window=1 << 23) as j:
+        rad = j.lazy_execute_batch(left, right, descs)
+    for g, r, w in zip(got, rad, want):
+        assert (g["count"], g["prod"]) == (w["count"], w["prod"]) == (r["count"], r["prod"])
+
+
 def test_learned_compacts_light_tuples_of_heavy_windows(lib, oracle):
     """At z = 1.5 most tuples carry a heavy key: the counting pass compacts the
     light ones and only those are partitioned; several windows of different
