@@ -244,7 +244,7 @@ def bench_batched(args, sjbg, torch, dev):
                   "hash_radix_partitioned": {"value": tuples / (ms_r * 1e-3), "ms_per_step": ms_r},
                   "outputs_identical_hash_vs_sort_merge": same, "outputs_identical_hash_vs_radix": same_r,
                   "tuples_per_step": tuples,
-                  "notes": "hash join autotuned + CUDA-graph replay; sort-merge graph replay (4 radix passes)"})
+                  "notes": "hash join autotuned + CUDA-graph replay; sort-merge graph replay (radix passes whose digit is zero in every key skip themselves on the device)"})
 
 
 def sjbg_log_uniform(w, lo=1 << 10, hi=1 << 20, seed=4):

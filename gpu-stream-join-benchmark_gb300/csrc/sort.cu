@@ -82,6 +82,30 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // ------------------------------------------------------------------ kernels
+// Under graph capture every pass is launched and the largest key (written on
+// the device by sort_max) decides: a pass whose digit is zero in every key is
+// the identity permutation and is skipped by all its kernels.  kmax == nullptr:
+// the host chose the passes.
+__device__ __forceinline__ bool pass_is_identity(const uint32_t *kmax, uint32_t shift) {
+    return kmax != nullptr && shift != 0 && (*kmax >> shift) == 0;
+}
+
+// After all four passes were launched: the passes that ran leave the result
+// in the scratch buffers when their number is odd; copy it home then.
+__global__ void __launch_bounds__(256)
+sort_home_kernel(uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, const uint32_t *__restrict__ keys2,
+                 const uint32_t *__restrict__ vals2, uint64_t n4, const uint32_t *__restrict__ kmax) {
+    const uint32_t m = *kmax;
+    uint32_t ran = 1;   // the first pass always runs
+    for (uint32_t shift = 8; shift < 32; shift += 8) ran += (m >> shift) != 0;
+    if ((ran & 1u) == 0) return;   // whole grid
+    uint4 *k4 = reinterpret_cast<uint4 *>(keys), *v4 = reinterpret_cast<uint4 *>(vals);
+    const uint4 *k24 = reinterpret_cast<const uint4 *>(keys2), *v24 = reinterpret_cast<const uint4 *>(vals2);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x) {
+        k4[i] = k24[i];
+        v4[i] = v24[i];
+    }
+}
 // Lanes of the warp holding the same 9-bit digit (256 = no element): one
 // ballot per bit, each lane keeping the lanes that agree with it on that bit.
 __device__ __forceinline__ unsigned digit_peers(uint32_t d) {
@@ -132,8 +156,10 @@ sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ s
 
 // counts block of segment s: counts[tile0 * 256 + d * ntiles + t_local]
 __global__ void __launch_bounds__(256)
-rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t shift,
-                  uint32_t *__restrict__ counts) {
+rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ segs,
+                  const uint32_t *__restrict__ tile_seg, uint32_t shift, uint32_t *__restrict__ counts,
+                  const uint32_t *__restrict__ kmax) {
+    if (pass_is_identity(kmax, shift)) return;   // whole grid
     __shared__ uint32_t hist[kDigits];
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
@@ -165,7 +191,9 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
 
 // One CTA per segment: exclusive scan of its 256 * ntiles counts in place.
 __global__ void __launch_bounds__(1024)
-rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs) {
+rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs, uint32_t shift,
+               const uint32_t *__restrict__ kmax) {
+    if (pass_is_identity(kmax, shift)) return;   // whole grid
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t carry_s;
     const SortSeg sg = segs[blockIdx.x];
@@ -221,7 +249,9 @@ __global__ void __launch_bounds__(kSortThreads)
 rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
                     const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t shift,
-                    const uint32_t *__restrict__ counts, uint32_t *__restrict__ status) {
+                    const uint32_t *__restrict__ counts, uint32_t *__restrict__ status,
+                    const uint32_t *__restrict__ kmax) {
+    if (pass_is_identity(kmax, shift)) return;   // whole grid
     extern __shared__ __align__(128) uint8_t smem_raw[];
     DownSmem &sm = *reinterpret_cast<DownSmem *>(smem_raw);
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
@@ -407,33 +437,41 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
     uint32_t *counts = static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * plan.tiles));
     uint32_t *hMax = static_cast<uint32_t *>(pinned_get(h, 5, 64));
     if (!dMax || !counts || !hMax) return fail(h, SJBG_E_NOMEM, "sort buffers");
-    uint32_t maxk = 0xFFFFFFFFu;   // under graph capture the key range is not read back: all 4 passes
+    SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
+    SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
+                      plan.tile_seg, dMax));
+    // outside graph capture the key range is read back and only the passes
+    // needed are launched; under capture all four are, and each skips itself
+    // on the device when its digit is zero in every key
+    uint32_t passes = 4;
+    const uint32_t *dkmax = dMax;
     if (!h->capturing) {
-        SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
-        SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys,
-                          dSegs, plan.tile_seg, dMax));
         SJBG_CK(h, cudaMemcpyAsync(hMax, dMax, 8, cudaMemcpyDeviceToHost, h->stream));
         SJBG_CK(h, cudaStreamSynchronize(h->stream));
-        maxk = hMax[0];
+        uint32_t bits = 0;
+        while (bits < 32 && (hMax[0] >> bits)) bits++;
+        passes = (bits + 7) / 8;
+        dkmax = nullptr;
     }
-    uint32_t bits = 0;
-    while (bits < 32 && (maxk >> bits)) bits++;
-    const uint32_t passes = (bits + 7) / 8;
     const size_t smem = sizeof(DownSmem);
     allow_big_smem(rs_downsweep_kernel, smem);
     uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
     for (uint32_t p = 0; p < passes; p++) {
         const uint32_t shift = 8 * p;
         SJBG_CK(h, launch(h, "rs_upsweep", rs_upsweep_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)kin,
-                          dSegs, plan.tile_seg, shift, counts));
-        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs));
+                          dSegs, plan.tile_seg, shift, counts, dkmax));
+        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs, shift, dkmax));
         SJBG_CK(h, launch(h, "rs_downsweep", rs_downsweep_kernel, dim3(plan.tiles), dim3(kSortThreads), smem,
                           (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, plan.tile_seg, shift,
-                          (const uint32_t *)counts, status));
+                          (const uint32_t *)counts, status, dkmax));
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    if (kin != keys) {   // odd number of passes: bring the result home
+    if (dkmax) {   // captured: the device knows how many passes ran
+        const uint64_t n4 = plan.elems / 4;   // segments are whole 4,096-element tiles
+        SJBG_CK(h, launch(h, "sort_home", sort_home_kernel, dim3((uint32_t)std::min<uint64_t>((n4 + 255) / 256, 8u * h->num_sms)),
+                          dim3(256), 0, keys, vals, (const uint32_t *)keys2, (const uint32_t *)vals2, n4, dkmax));
+    } else if (kin != keys) {   // odd number of passes: bring the result home
         SJBG_CK(h, cudaMemcpyAsync(keys, kin, sizeof(uint32_t) * plan.elems, cudaMemcpyDeviceToDevice, h->stream));
         SJBG_CK(h, cudaMemcpyAsync(vals, vin, sizeof(uint32_t) * plan.elems, cudaMemcpyDeviceToDevice, h->stream));
     }
