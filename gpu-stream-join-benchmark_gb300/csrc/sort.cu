@@ -2,7 +2,7 @@
 // segmented prefix sums, for the sort-merge join (sm_103a).
 //
 // One pass = three launches over all segments of a batch:
-//   rs_upsweep    per 4096-key tile: digit histogram (shared atomics)
+//   rs_upsweep    per 4096-key tile: digit histogram (one shared atomic per key)
 //   rs_scan       per segment: exclusive scan of its [256 digits x tiles]
 //                 count block, digit-major, so tile t's digit d lands after all
 //                 smaller digits and after digit d of tiles < t (stability)
@@ -180,9 +180,7 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
         for (int c = 0; c < 4; c++) {
             const bool valid = e0 + c < sg.n;
             const uint32_t d = valid ? (kk[c] >> shift) & 0xFFu : 0u;
-            // skewed keys share digits: combine equal digits of the warp first
-            const unsigned grp = digit_peers(valid ? d : 0x100u);
-            if (valid && lane_id() == (uint32_t)(__ffs(grp) - 1)) atomicAdd(&hist[d], (uint32_t)__popc(grp));
+            if (valid) atomicAdd(&hist[d], 1u);   // one shared atomic per key: faster than combining a warp's equal digits first
         }
     }
     SJBG_BARRIER();
