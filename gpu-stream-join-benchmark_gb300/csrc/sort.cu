@@ -151,7 +151,15 @@ sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ s
     for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x)
         if (base + i < sg.n) m = max(m, keys[sg.off + base + i]);
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-    if (lane_id() == 0 && m) atomicMax(out, m);
+    // one atomic per CTA, and only when it can raise the value seen (a stale
+    // read only costs an atomic: atomicMax decides)
+    __shared__ uint32_t wm[8];
+    if (lane_id() == 0) wm[warp_id()] = m;
+    SJBG_BARRIER();
+    if (threadIdx.x == 0) {
+        for (uint32_t q = 1; q < blockDim.x / 32; q++) m = max(m, wm[q]);
+        if (m > *(volatile const uint32_t *)out) atomicMax(out, m);
+    }
 }
 
 // counts block of segment s: counts[tile0 * 256 + d * ntiles + t_local]
@@ -378,30 +386,38 @@ __global__ void fr_seg_scan_kernel(unsigned long long *__restrict__ tsum, const 
 __global__ void __launch_bounds__(256)
 fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg,
                     const unsigned long long *__restrict__ tsum, unsigned long long *__restrict__ out) {
-    __shared__ unsigned long long wsum[8];
+    // warp w owns the tile's elements [w * 512, (w + 1) * 512), 32 consecutive
+    // ones per round: coalesced loads and stores, fr computed once per element
+    constexpr uint32_t kWarps = 8, kChunk = kSortTile / kWarps, kRounds = kChunk / 32;   // 256 threads
+    __shared__ unsigned long long wtot[kWarps];
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
-    constexpr uint32_t kPer = kSortTile / 256;   // 16 consecutive elements per thread
-    const uint32_t b0 = threadIdx.x * kPer;
-    unsigned long long loc = 0;
-    for (uint32_t i = 0; i < kPer; i++)
-        if (base + b0 + i < sg.n) loc += sjbg_fr(vals[sg.off + base + b0 + i]);
-    // exclusive scan of loc across the block
-    unsigned long long x = loc;
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane_id() >= (uint32_t)o) x += y;
+    const uint32_t w = warp_id(), lane = lane_id();
+    const uint32_t c0 = base + w * kChunk;
+    unsigned long long f[kRounds], tot = 0;
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; r++) {
+        const uint32_t li = c0 + 32 * r + lane;
+        f[r] = li < sg.n ? sjbg_fr(vals[sg.off + li]) : 0ull;
+        tot += f[r];
     }
-    if (lane_id() == 31) wsum[warp_id()] = x;
+    tot = warp_sum_u64(tot);
+    if (lane == 0) wtot[w] = tot;
     SJBG_BARRIER();
-    unsigned long long wofs = 0;
-    for (uint32_t ww = 0; ww < warp_id(); ww++) wofs += wsum[ww];
-    unsigned long long run = tsum[blockIdx.x] + wofs + x - loc;
-    for (uint32_t i = 0; i < kPer; i++) {
-        const uint32_t li = base + b0 + i;
-        if (li <= sg.n) out[sg.off + li] = run;   // positions 0..n inclusive
-        if (li < sg.n) run += sjbg_fr(vals[sg.off + li]);
+    unsigned long long run = tsum[blockIdx.x];
+    for (uint32_t ww = 0; ww < w; ww++) run += wtot[ww];
+#pragma unroll
+    for (uint32_t r = 0; r < kRounds; r++) {
+        unsigned long long x = f[r];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        const uint32_t li = c0 + 32 * r + lane;
+        if (li <= sg.n) out[sg.off + li] = run + x - f[r];   // positions 0..n inclusive
+        run += __shfl_sync(0xFFFFFFFFu, x, 31);
     }
 }
 
