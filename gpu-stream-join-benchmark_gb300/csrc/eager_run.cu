@@ -64,8 +64,9 @@ egather_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ 
 
 // Right-side tuples per sort tile.
 __global__ void __launch_bounds__(256)
-etile_count_kernel(const uint32_t *__restrict__ tags, const SortSeg *__restrict__ segs,
+etile_count_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
                    const uint32_t *__restrict__ tile_seg, uint32_t *__restrict__ tcount) {
+    const uint32_t *__restrict__ tags = view->vals;
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
@@ -114,7 +115,7 @@ __device__ __forceinline__ uint32_t eright_before_warp(const uint32_t *tags, con
 // Per sort tile: each tuple's count = other-side tuples before it in its key
 // group, summed into its batch's counter.
 __global__ void __launch_bounds__(kAttrThreads)
-eattr_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ tags, const SortSeg *__restrict__ segs,
+eattr_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
              const uint32_t *__restrict__ tile_seg, const ESegMeta *__restrict__ meta, const uint32_t *__restrict__ tpre,
              unsigned long long *__restrict__ counts) {
     extern __shared__ __align__(16) uint8_t attr_smem[];
@@ -124,6 +125,8 @@ eattr_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ tag
     int32_t *gst = reinterpret_cast<int32_t *>(rloc + kSortTile);                  // group start inside the tile, or -1
     __shared__ uint32_t warp_tot[kAttrThreads / 32];
     __shared__ uint32_t g0_s, r0_s;
+    const uint32_t *__restrict__ keys = view->keys;   // the sorted keys and their tags
+    const uint32_t *__restrict__ tags = view->vals;
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const ESegMeta m = meta[s];
@@ -333,17 +336,17 @@ int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr
     if (int rc_map = sort_tile_map(h, plan, dSegs)) return rc_map;
     SJBG_CK(h, launch(h, "erun_gather", egather_kernel, dim3((uint32_t)gat.size()), dim3(256), 0, dl, dr, dGat,
                       (uint32_t)B, k0, t0));
-    int rc = radix_sort_segments(h, plan, dSegs, k0, t0, k1, t1, reinterpret_cast<uint32_t *>(&dWin[nw].info));
+    const SortView *view = nullptr;
+    int rc = radix_sort_segments(h, plan, dSegs, k0, t0, k1, t1, reinterpret_cast<uint32_t *>(&dWin[nw].info), &view);
     if (rc) return rc;
     uint32_t *tpre = tcnt + std::max(plan.tiles, 1u);
-    SJBG_CK(h, launch(h, "erun_tile_count", etile_count_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)t0,
-                      dSegs, plan.tile_seg, tcnt));
+    SJBG_CK(h, launch(h, "erun_tile_count", etile_count_kernel, dim3(plan.tiles), dim3(256), 0, view, dSegs,
+                      plan.tile_seg, tcnt));
     SJBG_CK(h, launch(h, "erun_tile_scan", etile_scan_kernel, dim3(nw), dim3(32), 0, dSegs, nw,
                       (const uint32_t *)tcnt, tpre));
     allow_big_smem(eattr_kernel, kAttrSmem);
     SJBG_CK(h, launch(h, "erun_attribute", eattr_kernel, dim3(plan.tiles), dim3(kAttrThreads), kAttrSmem,
-                      (const uint32_t *)k0, (const uint32_t *)t0, dSegs, plan.tile_seg, dMeta, (const uint32_t *)tpre,
-                      dCounts));
+                      view, dSegs, plan.tile_seg, dMeta, (const uint32_t *)tpre, dCounts));
 
     uint32_t pu = 0;
     if (h->cfg.algorithm == SJBG_ALG_SMJ) return smj_lazy_batch(h, dl, dr, wh.data(), nw, nullptr, dWin, enumerate);

@@ -22,7 +22,7 @@ enum WsSlot : int {
     WS_BUCKET_CNT, WS_BUCKET_START, WS_BUCKET_CURSOR, WS_BUCKET_WIN,
     WS_WIN_PLAN, WS_TILE_PREFIX, WS_WIN_ACC, WS_PAIRS, WS_STATUS,
     WS_MODEL, WS_SAMPLE, WS_SAMPLE_KEYS, WS_HEAVY, WS_AUX0, WS_AUX1, WS_AUX2, WS_AUX3,
-    WS_SORT_K0, WS_SORT_K1, WS_SORT_V0, WS_SORT_V1, WS_SORT_HIST, WS_SORT_MAP,
+    WS_SORT_K0, WS_SORT_K1, WS_SORT_V0, WS_SORT_V1, WS_SORT_HIST, WS_SORT_MAP, WS_SORT_VIEW,
     WS_GEN_TABLE,
     WS_COMPACT, WS_COMPACT_CNT,      // light tuples written by the counting pass
     WS_COARSE_ROWS,                  // per tile: coarse-partition offsets of its light tuples

@@ -63,8 +63,9 @@ __device__ __forceinline__ uint32_t corank(const uint32_t *A, uint32_t na, const
 }
 
 // One thread per cut (all windows): cuts[cut0 + t] = co-rank of diagonal t * kMergeTile (clamped).
-__global__ void merge_corank_kernel(const uint32_t *__restrict__ keys, const MergeWin *__restrict__ wins, uint32_t nwin,
+__global__ void merge_corank_kernel(const SortView *__restrict__ view, const MergeWin *__restrict__ wins, uint32_t nwin,
                                     uint32_t total_cuts, uint32_t *__restrict__ cuts) {
+    const uint32_t *__restrict__ keys = view->keys;
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= total_cuts) return;
     uint32_t lo = 0, hi = nwin;   // window owning cut c: largest w with cut0 <= c
@@ -82,9 +83,11 @@ __global__ void merge_corank_kernel(const uint32_t *__restrict__ keys, const Mer
 
 template <bool kEnum, bool kPairs>
 __global__ void __launch_bounds__(kMergeThreads)
-merge_join_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
-                  const unsigned long long *__restrict__ F, const MergeWin *__restrict__ wins, uint32_t nwin,
-                  const uint32_t *__restrict__ cuts, WinAcc *__restrict__ acc, sjbg_pair *__restrict__ pairs) {
+merge_join_kernel(const SortView *__restrict__ view, const unsigned long long *__restrict__ F,
+                  const MergeWin *__restrict__ wins, uint32_t nwin, const uint32_t *__restrict__ cuts,
+                  WinAcc *__restrict__ acc, sjbg_pair *__restrict__ pairs) {
+    const uint32_t *__restrict__ keys = view->keys;
+    const uint32_t *__restrict__ vals = view->vals;
     __shared__ uint32_t sa[kMergeTile];
     const uint32_t w = find_merge_win(wins, nwin, blockIdx.x);
     const MergeWin mw = wins[w];
@@ -205,24 +208,25 @@ int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
     const MergeWin *dMw = reinterpret_cast<const MergeWin *>(dev + segB);
     if (int rc_map = sort_tile_map(h, plan, dSegs)) return rc_map;
 
+    const SortView *view = nullptr;
     int rc = sort_extract(h, dL, dR, n, plan, dSegs, k0, v0);
-    if (!rc) rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1, reinterpret_cast<uint32_t *>(&acc[n].info));
-    if (!rc) rc = segmented_fr_prefix(h, plan, n, dSegs, v0, F);
+    if (!rc) rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1, reinterpret_cast<uint32_t *>(&acc[n].info), &view);
+    if (!rc) rc = segmented_fr_prefix(h, plan, n, dSegs, view, F);
     if (rc) return rc;
     if (tiles == 0) return SJBG_OK;
     SJBG_CK(h, launch(h, "merge_corank", merge_corank_kernel, dim3((cuts + 255) / 256), dim3(256), 0,
-                      (const uint32_t *)k0, dMw, n, cuts, dCuts));
+                      view, dMw, n, cuts, dCuts));
     if (dPairs)
         SJBG_CK(h, launch(h, "merge_join_pairs", merge_join_kernel<true, true>, dim3(tiles), dim3(kMergeThreads), 0,
-                          (const uint32_t *)k0, (const uint32_t *)v0, (const unsigned long long *)F, dMw, n,
+                          view, (const unsigned long long *)F, dMw, n,
                           (const uint32_t *)dCuts, acc, dPairs));
     else if (enumerate)
         SJBG_CK(h, launch(h, "merge_join_xor", merge_join_kernel<true, false>, dim3(tiles), dim3(kMergeThreads), 0,
-                          (const uint32_t *)k0, (const uint32_t *)v0, (const unsigned long long *)F, dMw, n,
+                          view, (const unsigned long long *)F, dMw, n,
                           (const uint32_t *)dCuts, acc, dPairs));
     else
         SJBG_CK(h, launch(h, "merge_join_count", merge_join_kernel<false, false>, dim3(tiles), dim3(kMergeThreads), 0,
-                          (const uint32_t *)k0, (const uint32_t *)v0, (const unsigned long long *)F, dMw, n,
+                          view, (const unsigned long long *)F, dMw, n,
                           (const uint32_t *)dCuts, acc, dPairs));
     return SJBG_OK;
 }

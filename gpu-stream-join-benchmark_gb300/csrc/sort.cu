@@ -90,21 +90,20 @@ __device__ __forceinline__ bool pass_is_identity(const uint32_t *kmax, uint32_t 
     return kmax != nullptr && shift != 0 && (*kmax >> shift) == 0;
 }
 
-// After all four passes were launched: the passes that ran leave the result
-// in the scratch buffers when their number is odd; copy it home then.
-__global__ void __launch_bounds__(256)
-sort_home_kernel(uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, const uint32_t *__restrict__ keys2,
-                 const uint32_t *__restrict__ vals2, uint64_t n4, const uint32_t *__restrict__ kmax) {
-    const uint32_t m = *kmax;
-    uint32_t ran = 1;   // the first pass always runs
-    for (uint32_t shift = 8; shift < 32; shift += 8) ran += (m >> shift) != 0;
-    if ((ran & 1u) == 0) return;   // whole grid
-    uint4 *k4 = reinterpret_cast<uint4 *>(keys), *v4 = reinterpret_cast<uint4 *>(vals);
-    const uint4 *k24 = reinterpret_cast<const uint4 *>(keys2), *v24 = reinterpret_cast<const uint4 *>(vals2);
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x) {
-        k4[i] = k24[i];
-        v4[i] = v24[i];
+// Points the view at the buffer pair the last pass wrote: after an even
+// number of passes the input pair, after an odd number the scratch pair.
+// kmax == nullptr: the host's pass count `passes` ran; else the first pass and
+// every pass whose digit is not zero in the largest key did.
+__global__ void sort_view_kernel(SortView *view, const uint32_t *keys, const uint32_t *vals, const uint32_t *keys2,
+                                 const uint32_t *vals2, const uint32_t *__restrict__ kmax, uint32_t passes) {
+    uint32_t ran = passes;
+    if (kmax) {
+        const uint32_t m = *kmax;
+        ran = 1;
+        for (uint32_t shift = 8; shift < 32; shift += 8) ran += (m >> shift) != 0;
     }
+    view->keys = (ran & 1u) ? keys2 : keys;
+    view->vals = (ran & 1u) ? vals2 : vals;
 }
 // Lanes of the warp holding the same 9-bit digit (256 = no element): one
 // ballot per bit, each lane keeping the lanes that agree with it on that bit.
@@ -352,8 +351,9 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
 // ---- segmented exclusive prefix of fr(val): tile sums, per-segment scan of the
 // ---- tile sums, per-tile scan plus offset
 __global__ void __launch_bounds__(256)
-fr_tile_sum_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg,
-                   unsigned long long *__restrict__ tsum) {
+fr_tile_sum_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
+                   const uint32_t *__restrict__ tile_seg, unsigned long long *__restrict__ tsum) {
+    const uint32_t *__restrict__ vals = view->vals;
     __shared__ unsigned long long ws[8];
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
@@ -384,8 +384,10 @@ __global__ void fr_seg_scan_kernel(unsigned long long *__restrict__ tsum, const 
 }
 
 __global__ void __launch_bounds__(256)
-fr_tile_scan_kernel(const uint32_t *__restrict__ vals, const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg,
-                    const unsigned long long *__restrict__ tsum, unsigned long long *__restrict__ out) {
+fr_tile_scan_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
+                    const uint32_t *__restrict__ tile_seg, const unsigned long long *__restrict__ tsum,
+                    unsigned long long *__restrict__ out) {
+    const uint32_t *__restrict__ vals = view->vals;
     // warp w owns the tile's elements [w * 512, (w + 1) * 512), 32 consecutive
     // ones per round: coalesced loads and stores, fr computed once per element
     constexpr uint32_t kWarps = 8, kChunk = kSortTile / kWarps, kRounds = kChunk / 32;   // 256 threads
@@ -445,12 +447,13 @@ int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB,
 }
 
 int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
-                        uint32_t *keys2, uint32_t *vals2, uint32_t *status) {
+                        uint32_t *keys2, uint32_t *vals2, uint32_t *status, const SortView **view) {
     const uint32_t nseg = (uint32_t)plan.segs.size();
     uint32_t *dMax = static_cast<uint32_t *>(ws_get(h, WS_STATUS, 64));
     uint32_t *counts = static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * plan.tiles));
     uint32_t *hMax = static_cast<uint32_t *>(pinned_get(h, 5, 64));
-    if (!dMax || !counts || !hMax) return fail(h, SJBG_E_NOMEM, "sort buffers");
+    SortView *dView = static_cast<SortView *>(ws_get(h, WS_SORT_VIEW, sizeof(SortView)));
+    if (!dMax || !counts || !hMax || !dView) return fail(h, SJBG_E_NOMEM, "sort buffers");
     SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
     SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
                       plan.tile_seg, dMax));
@@ -481,27 +484,23 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    if (dkmax) {   // captured: the device knows how many passes ran
-        const uint64_t n4 = plan.elems / 4;   // segments are whole 4,096-element tiles
-        SJBG_CK(h, launch(h, "sort_home", sort_home_kernel, dim3((uint32_t)std::min<uint64_t>((n4 + 255) / 256, 8u * h->num_sms)),
-                          dim3(256), 0, keys, vals, (const uint32_t *)keys2, (const uint32_t *)vals2, n4, dkmax));
-    } else if (kin != keys) {   // odd number of passes: bring the result home
-        SJBG_CK(h, cudaMemcpyAsync(keys, kin, sizeof(uint32_t) * plan.elems, cudaMemcpyDeviceToDevice, h->stream));
-        SJBG_CK(h, cudaMemcpyAsync(vals, vin, sizeof(uint32_t) * plan.elems, cudaMemcpyDeviceToDevice, h->stream));
-    }
+    // no copy home: the consumers read the result where the last pass left it
+    SJBG_CK(h, launch(h, "sort_view", sort_view_kernel, dim3(1), dim3(1), 0, dView, (const uint32_t *)keys,
+                      (const uint32_t *)vals, (const uint32_t *)keys2, (const uint32_t *)vals2, dkmax, passes));
+    *view = dView;
     return SJBG_OK;
 }
 
 int segmented_fr_prefix(sjbg_handle *h, const SortPlan &plan, uint32_t nseg, const SortSeg *dSegs,
-                        const uint32_t *vals, unsigned long long *out) {
+                        const SortView *view, unsigned long long *out) {
     if (nseg == 0) return SJBG_OK;
     // the first nseg segments: their tiles are [0, tile0 of segment nseg)
     const uint32_t tiles = nseg < plan.segs.size() ? plan.segs[nseg].tile0 : plan.tiles;
     unsigned long long *tsum = static_cast<unsigned long long *>(ws_get(h, WS_AUX3, sizeof(unsigned long long) * tiles));
     if (!tsum) return fail(h, SJBG_E_NOMEM, "prefix buffers");
-    SJBG_CK(h, launch(h, "fr_tile_sum", fr_tile_sum_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, plan.tile_seg, tsum));
+    SJBG_CK(h, launch(h, "fr_tile_sum", fr_tile_sum_kernel, dim3(tiles), dim3(256), 0, view, dSegs, plan.tile_seg, tsum));
     SJBG_CK(h, launch(h, "fr_seg_scan", fr_seg_scan_kernel, dim3(nseg), dim3(32), 0, tsum, dSegs));
-    SJBG_CK(h, launch(h, "fr_tile_scan", fr_tile_scan_kernel, dim3(tiles), dim3(256), 0, vals, dSegs, plan.tile_seg,
+    SJBG_CK(h, launch(h, "fr_tile_scan", fr_tile_scan_kernel, dim3(tiles), dim3(256), 0, view, dSegs, plan.tile_seg,
                       (const unsigned long long *)tsum, out));
     return SJBG_OK;
 }

@@ -45,16 +45,27 @@ int sort_tile_map(sjbg_handle *h, SortPlan &plan, const SortSeg *dSegs);
 
 __device__ __forceinline__ uint32_t find_seg(const uint32_t *tile_seg, uint32_t tile) { return tile_seg[tile]; }
 
-// Stable LSD sort of every segment by key; keys/vals hold the input and the
-// sorted result on return (keys2/vals2 are scratch).  Passes = ceil(bits/8)
-// where bits covers the largest key (read back once).
+// Where a sort's result lies (device memory, written by the sort): the
+// passes alternate between the two buffer pairs, and under graph capture only
+// the device knows how many ran.
+struct SortView {
+    const uint32_t *keys;
+    const uint32_t *vals;
+};
+
+// Stable LSD sort of every segment by key; keys/vals hold the input, and the
+// result is in keys/vals or keys2/vals2 as *view (a device pointer) says.
+// Outside graph capture the passes are ceil(bits/8) where bits covers the
+// largest key (read back once); under capture each pass skips itself on the
+// device when its digit is zero in every key.
 // status: a device word that receives kErrTimeout if a tile's bulk copy never lands.
 int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
-                        uint32_t *keys2, uint32_t *vals2, uint32_t *status);
+                        uint32_t *keys2, uint32_t *vals2, uint32_t *status, const SortView **view);
 
 // Exclusive prefix sums of fr(val) (u64, mod 2^64) of the first nseg
-// segments into out (same padded layout; positions 0..n of each segment).
+// segments into out (same padded layout; positions 0..n of each segment);
+// vals are the sort's (view).
 int segmented_fr_prefix(sjbg_handle *h, const SortPlan &plan, uint32_t nseg, const SortSeg *dSegs,
-                        const uint32_t *vals, unsigned long long *out);
+                        const SortView *view, unsigned long long *out);
 
 }  // namespace sjbg
