@@ -35,6 +35,57 @@ struct NljItem {
     uint32_t win, l0, r0, pad;
 };
 
+// Whether any of the thread's 8 left keys equals any of 4 right keys: the 32
+// compares as PTX setp.eq with an OR into the predicate (one instruction per
+// compare), in four independent chains (one per right key) merged at the end.
+static_assert(kLReg == 8, "any_equal_8x4 compares 8 left keys");
+__device__ __forceinline__ uint32_t any_equal_8x4(const uint32_t (&l)[kLReg], const uint4 k) {
+    uint32_t hit;
+    asm("{\n\t"
+        ".reg .pred p0, p1, p2, p3;\n\t"
+        "setp.eq.u32 p0, %1, %9;\n\t"
+        "setp.eq.u32 p1, %1, %10;\n\t"
+        "setp.eq.u32 p2, %1, %11;\n\t"
+        "setp.eq.u32 p3, %1, %12;\n\t"
+        "setp.eq.or.u32 p0, %2, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %2, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %2, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %2, %12, p3;\n\t"
+        "setp.eq.or.u32 p0, %3, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %3, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %3, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %3, %12, p3;\n\t"
+        "setp.eq.or.u32 p0, %4, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %4, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %4, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %4, %12, p3;\n\t"
+        "setp.eq.or.u32 p0, %5, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %5, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %5, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %5, %12, p3;\n\t"
+        "setp.eq.or.u32 p0, %6, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %6, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %6, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %6, %12, p3;\n\t"
+        "setp.eq.or.u32 p0, %7, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %7, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %7, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %7, %12, p3;\n\t"
+        "setp.eq.or.u32 p0, %8, %9, p0;\n\t"
+        "setp.eq.or.u32 p1, %8, %10, p1;\n\t"
+        "setp.eq.or.u32 p2, %8, %11, p2;\n\t"
+        "setp.eq.or.u32 p3, %8, %12, p3;\n\t"
+        "or.pred p0, p0, p1;\n\t"
+        "or.pred p2, p2, p3;\n\t"
+        "or.pred p0, p0, p2;\n\t"
+        "selp.u32 %0, 1, 0, p0;\n\t"
+        "}"
+        : "=r"(hit)
+        : "r"(l[0]), "r"(l[1]), "r"(l[2]), "r"(l[3]), "r"(l[4]), "r"(l[5]), "r"(l[6]), "r"(l[7]), "r"(k.x),
+          "r"(k.y), "r"(k.z), "r"(k.w));
+    return hit;
+}
+
 // One CTA's share of a window: left tuples [l0, l0 + kLTile) against right
 // tuples [r0, r0 + kRSplit).  Adds count/xor/prod to *acc (and the count to
 // *extra_count when given); pairs go to pout[0, pcap) via *npairs.
@@ -86,9 +137,7 @@ __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uin
 #pragma unroll 4
             for (uint32_t q = 0; q < kVote / 4; q++) {
                 const uint4 k4 = rk4[(r >> 2) + q];
-#pragma unroll
-                for (int a = 0; a < kLReg; a++)
-                    p |= (lk[a] == k4.x) | (lk[a] == k4.y) | (lk[a] == k4.z) | (lk[a] == k4.w);
+                p |= any_equal_8x4(lk, k4) != 0u;
             }
             if (!__any_sync(0xFFFFFFFFu, p)) continue;
             // exact path for this group of kVote right keys (warp-uniform)
