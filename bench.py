@@ -604,6 +604,7 @@ def main():
                       "partitioner": "none: one open-addressing table per window in HBM"},
         "learned_over_plain": ms_plain / ms_learned,
         "learned_windows": sum(1 for a in res_learned if a[2] == sjbg.PART_LEARNED),
+        "radix_by_cost_windows": sum(1 for a in res_learned if a[3] & sjbg.WR_RADIX_BY_COST),
         "outputs_identical_learned_vs_plain": same,   # and vs radix (learned fan-out) and the HBM table
         "latency": {"p50_ms": p50, "p99_ms": p99, "windows": len(lat), "unit": "ms per window call"},
         "e2e": {"value": tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": 32 * total,

@@ -191,9 +191,9 @@ static void fill_result(const sjbg_handle *h, const WinAcc &a, const WinHost &w,
     out->count = a.count;
     out->prod_checksum = a.prod;
     out->partitioner_used = part_used;
-    if (part_used == SJBG_PART_LEARNED && (a.info & kInfoFallback)) {
+    if (part_used == SJBG_PART_LEARNED && (a.info & (kInfoFallback | kInfoRadixByCost))) {
         out->partitioner_used = SJBG_PART_RADIX;
-        out->flags |= SJBG_WR_FALLBACK;
+        out->flags |= (a.info & kInfoFallback) ? SJBG_WR_FALLBACK : SJBG_WR_RADIX_BY_COST;
     }
     out->ms = ms;
     if (enumerate) {

@@ -38,7 +38,7 @@ struct WinAcc {
     unsigned long long info;     // kInfo* bits | heavy keys << 32 (learned partitioning)
 };
 
-enum : unsigned long long { kInfoLearned = 1ull, kInfoFallback = 2ull };
+enum : unsigned long long { kInfoLearned = 1ull, kInfoFallback = 2ull, kInfoRadixByCost = 4ull };
 
 // Per-window plan entry of a lazy batch, in device memory.
 struct WinPlan {

@@ -413,8 +413,8 @@ __global__ void heavy_finish_kernel(const WinPlan *__restrict__ wins, uint32_t n
     const uint32_t w = blockIdx.x;
     const WinPlan wp = wins[w];
     if (wp.model == 0xFFFFFFFFu) return;
-    if (models[wp.model].fallback) {
-        if (threadIdx.x == 0) acc[w].info = kInfoFallback;
+    if (models[wp.model].fallback) {   // 1: the model overflowed; 2: radix chosen by cost
+        if (threadIdx.x == 0) acc[w].info = models[wp.model].fallback == 2u ? kInfoRadixByCost : kInfoFallback;
         return;
     }
     const uint32_t nh = models[wp.model].n_heavy;

@@ -18,7 +18,9 @@
 //                  (centred sums, two passes); lo/hi clamps make it monotone.
 //   5. check       (inference) the model buckets the light sample; if the
 //                  largest predicted bucket exceeds overflow_bound times the
-//                  mean, the window falls back to radix partitioning.
+//                  mean, the window falls back to radix partitioning.  It also
+//                  keeps radix (by cost) when heavy keys hold little of the
+//                  sample and radix buckets the whole sample evenly.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -32,6 +34,12 @@ constexpr uint32_t kBins = 1u << 14;     // histogram bins of the fit (held in s
 constexpr uint32_t kCandMax = 2048;       // heavy candidates kept per window
 constexpr uint32_t kSampleThreads = 256;
 constexpr uint32_t kPredStride = 1u << 14;  // predicted-bucket counters per window (max buckets)
+// A window keeps radix partitioning (by cost) when heavy keys hold less than
+// this share of its sample and radix's largest sampled bucket is at most this
+// many times the mean: measured at z = 0.5 over 2^24 keys, the learned
+// classification then costs more per tuple than its buckets save.
+constexpr float kCostHeavyShare = 0.10f;
+constexpr float kCostRadixBalance = 2.0f;
 
 struct SampleWin {
     uint64_t left_off, n_left, right_off, n_right;
@@ -268,7 +276,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     __shared__ uint32_t warp_tot[32];
     __shared__ double rootpart[32][2];
     __shared__ float root_s[2];
-    __shared__ uint32_t n_heavy_s, light_total_s, log2_eff_s, compact_s;
+    __shared__ uint32_t n_heavy_s, light_total_s, log2_eff_s, compact_s, cost_s;
     __shared__ uint32_t cpre[kCandMax + 1];        // exclusive prefix of the sorted candidates' counts
     const uint32_t w = blockIdx.x;
     const SampleWin s = wins[w];
@@ -368,6 +376,7 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         // when at most half of the sample is light, the counting pass also
         // writes the light tuples out compacted, and only those are re-read
         compact_s = (h > 0 && 2 * light <= s.m) ? 1u : 0u;
+        cost_s = ((float)(s.m - light) < kCostHeavyShare * (float)s.m) ? 1u : 0u;
     }
     SJBG_BARRIER();
     const uint32_t nh = n_heavy_s;
@@ -532,13 +541,15 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
             M.leaves = leaves; M.log2_buckets = log2_eff_s; M.fallback = (total == 0 && nh == 0) ? 1u : 0u;
             M.n_heavy = nh;
             M.compact = compact_s;
+            M.cost_check = cost_s;
         }
     }
 }
 
 // Inference on the sample: predicted bucket sizes of the light keys.
 __global__ void __launch_bounds__(kSampleThreads)
-learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedModel *models, uint32_t *pred) {
+learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedModel *models, uint32_t *pred,
+                     uint32_t *prad) {
     __shared__ HeavySet hs;
     __shared__ LearnedCore core;
     const uint32_t w = blockIdx.y;
@@ -548,9 +559,12 @@ learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedM
     heavy_set_load(hs, m);
     copy_to_smem(&core, m, sizeof(LearnedCore));
     uint32_t *pw = pred + (uint64_t)w * kPredStride;
+    uint32_t *rw = prad + (uint64_t)w * kPredStride;
     const uint32_t *kw = keys + s.key_off;
+    const uint32_t rmask = (1u << s.log2_buckets) - 1u;   // radix on the plan's fan-out, every key
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.m; i += gridDim.x * blockDim.x) {
         const uint32_t k = kw[i];
+        if (core.cost_check) atomicAdd(&rw[k & rmask], 1u);
         if (heavy_find(hs, k) != kHeavyBucket) continue;
         atomicAdd(&pw[learned_bucket(core, k)], 1u);
     }
@@ -559,14 +573,14 @@ learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedM
 // One CTA per window: worst predicted bucket vs the mean -> fallback flag;
 // the window's plan is pointed at its model slot.
 __global__ void __launch_bounds__(1024)
-learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint32_t *pred, float bound,
-                        WinPlan *plan) {
-    __shared__ uint32_t mx_s, sum_s;
+learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint32_t *pred, const uint32_t *prad,
+                        float bound, WinPlan *plan) {
+    __shared__ uint32_t mx_s, sum_s, rmx_s;
     const uint32_t w = blockIdx.x;
     LearnedModel &M = models[w];
     if (threadIdx.x == 0) plan[w].model = w;
     if (M.fallback) return;
-    if (threadIdx.x == 0) { mx_s = 0; sum_s = 0; }
+    if (threadIdx.x == 0) { mx_s = 0; sum_s = 0; rmx_s = 0; }
     SJBG_BARRIER();
     const uint32_t P = 1u << M.log2_buckets;
     const uint32_t *pw = pred + (uint64_t)w * kPredStride;
@@ -574,11 +588,25 @@ learned_overflow_kernel(const SampleWin *wins, LearnedModel *models, const uint3
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) { mx = max(mx, pw[i]); sm += pw[i]; }
     atomicMax(&mx_s, mx);
     atomicAdd(&sum_s, sm);
+    // radix on the plan's fan-out, all sampled keys
+    const SampleWin s = wins[w];
+    const uint32_t PR = 1u << s.log2_buckets;
+    const uint32_t *rw = prad + (uint64_t)w * kPredStride;
+    uint32_t rmx = 0;
+    for (uint32_t i = threadIdx.x; i < PR; i += blockDim.x) rmx = max(rmx, rw[i]);
+    atomicMax(&rmx_s, rmx);
     SJBG_BARRIER();
     if (threadIdx.x == 0) {
         const float mean = (float)sum_s / (float)P;
         // a window whose light sample is too small to judge keeps its model
-        if (sum_s >= 4 * P && (float)mx_s > bound * mean) M.fallback = 1u;
+        if (sum_s >= 4 * P && (float)mx_s > bound * mean) {
+            M.fallback = 1u;
+        } else if (M.cost_check && s.m >= 4 * PR && (float)(s.m - sum_s) < kCostHeavyShare * (float)s.m &&
+                   (float)rmx_s * (float)PR <= kCostRadixBalance * (float)s.m) {
+            // heavy keys hold little of the sample and radix is balanced on it:
+            // the model's per-tuple work (set lookup, leaf line) costs more than it saves
+            M.fallback = 2u;
+        }
     }
 }
 
@@ -636,7 +664,8 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     const size_t candB = sizeof(unsigned long long) * (size_t)kCandMax * n, predB = sizeof(uint32_t) * (size_t)n * kPredStride;
     uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 1, swB + scB));
     uint8_t *dsmall = static_cast<uint8_t *>(ws_get(h, WS_SAMPLE, swB + scB));
-    uint32_t *dHist = static_cast<uint32_t *>(ws_get(h, WS_AUX0, histB + predB));
+    // sample histograms, then the model's and radix's predicted bucket counts
+    uint32_t *dHist = static_cast<uint32_t *>(ws_get(h, WS_AUX0, histB + 2 * predB));
     unsigned long long *dTab = static_cast<unsigned long long *>(ws_get(h, WS_AUX1, tabB));
     unsigned long long *dCand = static_cast<unsigned long long *>(ws_get(h, WS_AUX2, candB));
     LearnedModel *dM = static_cast<LearnedModel *>(ws_get(h, WS_MODEL, sizeof(LearnedModel) * n));
@@ -646,6 +675,7 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         return fail(h, SJBG_E_NOMEM, "learned partitioner buffers");
     uint32_t *dLists = dKeys + keys_total;
     uint32_t *dPred = dHist + (size_t)kBins * n;
+    uint32_t *dPrad = dPred + (size_t)n * kPredStride;
     std::memcpy(hst, sw.data(), swB);
     SampleScratch init;
     std::memset(&init, 0, sizeof(init));
@@ -653,7 +683,7 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     std::vector<SampleScratch> scr(n, init);
     std::memcpy(hst + swB, scr.data(), scB);
     if (int rc_up = stage_copy(h, dsmall, hst, swB + scB)) return rc_up;
-    SJBG_CK(h, cudaMemsetAsync(dHist, 0, histB + predB, h->stream));
+    SJBG_CK(h, cudaMemsetAsync(dHist, 0, histB + 2 * predB, h->stream));
     SJBG_CK(h, cudaMemsetAsync(dTab, 0, tabB, h->stream));
     const SampleWin *dSw = reinterpret_cast<const SampleWin *>(dsmall);
     SampleScratch *dScr = reinterpret_cast<SampleScratch *>(dsmall + swB);
@@ -673,9 +703,9 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
                       dHist, dCand, dM, leaves, allow_heavy ? kMaxHeavy : 0u, bound));
     const uint32_t bc = std::max<uint32_t>(1, std::min<uint32_t>(64, (max_m + 4095) / 4096));
     SJBG_CK(h, launch(h, "learned_check", learned_check_kernel, dim3(bc, n), dim3(kSampleThreads), 0,
-                      (const uint32_t *)dKeys, dSw, (const LearnedModel *)dM, dPred));
+                      (const uint32_t *)dKeys, dSw, (const LearnedModel *)dM, dPred, dPrad));
     SJBG_CK(h, launch(h, "learned_overflow", learned_overflow_kernel, dim3(n), dim3(1024), 0, dSw, dM,
-                      (const uint32_t *)dPred, bound, dPlan));
+                      (const uint32_t *)dPred, (const uint32_t *)dPrad, bound, dPlan));
     *dModels = dM;
     return SJBG_OK;
 }

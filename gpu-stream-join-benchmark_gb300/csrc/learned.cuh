@@ -47,7 +47,8 @@ struct __align__(16) LearnedCore {
     float kmin, inv_range, root_a, root_b;
     uint32_t leaves, log2_buckets, fallback, n_heavy;
     uint32_t compact;     // light tuples are compacted while counting (most tuples are heavy)
-    uint32_t pad_[3];
+    uint32_t cost_check;  // few heavy keys: the check also buckets the sample by radix (the cost rule)
+    uint32_t pad_[2];
     float4 leaf[kMaxLeaves];   // per leaf {slope, intercept, lo, hi}
 };
 

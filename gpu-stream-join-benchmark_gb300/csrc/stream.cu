@@ -108,10 +108,14 @@ static void harvest(sjbg_handle *h, StreamState &st, bool wait) {
             r.count = a.count;
             r.prod_checksum = a.prod;
             r.partitioner_used = w->part_used;
-            if (w->part_used == SJBG_PART_LEARNED && (a.info & kInfoFallback)) {
+            if (w->part_used == SJBG_PART_LEARNED && (a.info & (kInfoFallback | kInfoRadixByCost))) {
                 r.partitioner_used = SJBG_PART_RADIX;
-                r.flags |= SJBG_WR_FALLBACK;
-                st.fallbacks++;
+                if (a.info & kInfoFallback) {
+                    r.flags |= SJBG_WR_FALLBACK;
+                    st.fallbacks++;
+                } else {
+                    r.flags |= SJBG_WR_RADIX_BY_COST;
+                }
             }
             r.ms = lat;
             (void)busy;

@@ -29,7 +29,7 @@ RESULT_NO_OUTPUT, RESULT_COUNT_KERNEL, RESULT_ESTIMATED_SELECTIVITY, RESULT_BITM
 PART_AUTO, PART_NONE, PART_RADIX, PART_LEARNED = 0, 1, 2, 3
 MEM_HOST, MEM_DEVICE = 0, 1
 F_XOR, F_PROFILE, F_AUTOTUNE, F_VERIFY, F_GRAPH = 0x1, 0x2, 0x4, 0x8, 0x10
-WR_XOR, WR_PAIRS_TRUNCATED, WR_FALLBACK = 0x1, 0x2, 0x4
+WR_XOR, WR_PAIRS_TRUNCATED, WR_FALLBACK, WR_RADIX_BY_COST = 0x1, 0x2, 0x4, 0x8
 
 STATUS = {0: "OK", 1: "E_INVALID", 2: "E_NOMEM", 3: "E_CUDA", 4: "E_TIMEOUT", 5: "E_CAPACITY",
           6: "E_UNSUPPORTED", 7: "E_BUDGET", 8: "E_STATE", 9: "E_MISMATCH"}

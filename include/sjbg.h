@@ -121,6 +121,7 @@ enum { SJBG_MEM_HOST = 0, SJBG_MEM_DEVICE = 1 };
 #define SJBG_WR_XOR             0x1u /* xor_checksum is valid */
 #define SJBG_WR_PAIRS_TRUNCATED 0x2u /* more pairs than pairs_capacity; n_pairs = capacity */
 #define SJBG_WR_FALLBACK        0x4u /* learned model overflowed; radix was used */
+#define SJBG_WR_RADIX_BY_COST   0x8u /* learned partitioner chose radix: balanced on the sample, few heavy tuples */
 
 /* Executor configuration.  Field meanings follow the reference's
  * AlgorithmConfig / DataConfig / QueryConfig / EngineConfig

@@ -194,6 +194,22 @@ def test_learned_keeps_its_model_when_many_keys_are_hot(lib, oracle, z):
     assert (got["count"], got["prod"]) == (want["count"], want["prod"]) == (rad["count"], rad["prod"])
 
 
+def test_learned_keeps_radix_when_it_is_cheaper(lib, oracle):
+    """Zipf z = 0.5 over 2^24 keys: heavy keys hold well under a tenth of the
+    sample and radix buckets it evenly, so the learned partitioner keeps radix
+    partitioning (flagged, not a fallback) and the result equals the oracle."""
+    D, W = 1 << 24, 1 << 22
+    table = oracle.zipf_table(D, 0.5)
+    left = oracle.gen_zipf(0, W, 1, table, D, 3)
+    right = oracle.gen_zipf(0, W, 2, table, D, 3)
+    want = oracle.join(left, right, enumerate_pairs=False)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=W) as j:
+        got = j.lazy_execute(left, right)
+    assert got["partitioner_used"] == lib.PART_RADIX
+    assert got["flags"] & lib.WR_RADIX_BY_COST and not (got["flags"] & lib.WR_FALLBACK)
+    assert (got["count"], got["prod"]) == (want["count"], want["prod"])
+
+
 def test_learned_heavy_keys_sharing_a_set_bucket(lib, oracle):
     """The heavy-key set has 2,048 buckets of two slots (bucket = top 11 bits of
     key * 0x9E3779B97F4A7C15).  Four heavy keys of one bucket: the two heaviest
