@@ -916,10 +916,11 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
     if (nR == 0 || nS == 0) return;
     uint64_t *Rb = partL + start[b];
     const uint64_t *Sb = partR + start[B + b];
-    // the table holds at most nR distinct keys: 1.3x that many slots (load
-    // <= 0.77; at least 64, at most the launch's capacity) keep small buckets
-    // cheap to clear and let two CTAs share an SM
-    const uint32_t C = min(cap, max(64u, (nR * 13u / 10u + 31u) & ~31u));
+    // the table holds at most nR distinct keys: 2 slots per left tuple (at
+    // least 64, at most the launch's capacity of 1.3 per target tuple, which
+    // lets two CTAs share an SM), so buckets under the target probe at load
+    // <= 1/2: with mostly distinct keys a miss then walks ~3 slots, not ~10
+    const uint32_t C = min(cap, max(64u, (nR * 2u + 31u) & ~31u));
     CountTable t;
     t.sumf = reinterpret_cast<unsigned long long *>(smem_raw);
     t.keys = reinterpret_cast<uint32_t *>(t.sumf + C + 1);
