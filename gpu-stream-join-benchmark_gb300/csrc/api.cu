@@ -230,6 +230,7 @@ static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR
         SJBG_CK(h, cudaEventRecord(e0, h->stream));
         SJBG_CK(h, cudaGraphLaunch(entry->exec, h->stream));
         SJBG_CK(h, cudaEventRecord(e1, h->stream));
+        h->launches += entry->kernels;   // the replay runs every captured kernel again
         hAcc = static_cast<WinAcc *>(entry->pinned[3].p);
         part_used = entry->part_used;
     } else {
@@ -256,6 +257,7 @@ static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR
         }
         for (int i = 0; i < 6; i++) std::swap(h->pinned[i], e->pinned[i]);
         h->capturing = true;
+        const uint64_t launches_before = h->launches;
         cudaGraph_t graph = nullptr;
         cudaError_t ce = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed);
         uint32_t pu2 = 0;
@@ -264,6 +266,8 @@ static int lazy_graph(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR
                                     : SJBG_E_CUDA;
         cudaError_t ce2 = cudaStreamEndCapture(h->stream, &graph);
         h->capturing = false;
+        e->kernels = h->launches - launches_before;
+        h->launches = launches_before;   // capture runs nothing
         for (int i = 0; i < 6; i++) std::swap(h->pinned[i], e->pinned[i]);
         if (rc2 == SJBG_OK && ce == cudaSuccess && ce2 == cudaSuccess && graph) {
             if (cudaGraphInstantiate(&e->exec, graph, 0) != cudaSuccess) e->exec = nullptr;

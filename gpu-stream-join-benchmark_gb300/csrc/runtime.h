@@ -77,6 +77,7 @@ struct sjbg_handle {
         cudaGraphExec_t exec = nullptr;
         sjbg::DevBuf pinned[6];
         uint32_t part_used = 0;
+        uint64_t kernels = 0;   // kernel launches captured: counted again on every replay
     };
     std::vector<std::unique_ptr<GraphEntry>> graphs;
     std::map<std::string, Tune> tuned;   // autotuner decisions by workload shape

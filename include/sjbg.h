@@ -294,7 +294,8 @@ SJBG_API int sjbg_kernel_stats(sjbg_handle *h, uint32_t index, char *name, size_
                       uint64_t *launches, double *total_ms);
 SJBG_API int sjbg_kernel_stats_reset(sjbg_handle *h);
 
-/* Kernel launches issued by this handle since creation. */
+/* Kernel launches issued by this handle since creation (a replayed graph
+ * counts each kernel it runs). */
 SJBG_API uint64_t sjbg_launch_count(const sjbg_handle *h);
 
 #ifdef __cplusplus
