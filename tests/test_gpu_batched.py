@@ -41,6 +41,33 @@ def test_batched_graph_replay_matches_oracle(lib, oracle, tmp_path, algo):
         assert '"bucket_target"' in text and '"persistent"' in text
 
 
+def test_learned_graph_replay_reruns_every_kernel(lib, oracle):
+    """Learned partitioning under graph replay (the bench's throughput arms):
+    every replay re-samples and re-fits on the device and equals the first run
+    and the oracle; each replay counts its kernels again."""
+    torch = pytest.importorskip("torch")
+    D, W = 1 << 24, 1 << 20
+    table = oracle.zipf_table(D, 1.5)
+    left = np.concatenate([oracle.gen_zipf(w * W, W, 1, table, D, 3) for w in range(3)])
+    right = np.concatenate([oracle.gen_zipf(w * W, W, 2, table, D, 3) for w in range(3)])
+    descs = [(w * W, W, w * W, W, 0, 0) for w in range(3)]
+    want, _ = oracle.join_windows(left, right, descs, enumerate_pairs=False)
+    dl = torch.from_numpy(left.view(np.uint8)).cuda()
+    dr = torch.from_numpy(right.view(np.uint8)).cuda()
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, flags=lib.F_GRAPH,
+                    max_tuples_per_window=W) as j:
+        runs, counts = [], []
+        for _ in range(3):   # run + capture, then two replays
+            runs.append(j.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE))
+            counts.append(j.launch_count())
+    for run in runs:
+        for g, w in zip(run, want):
+            assert (g["count"], g["prod"]) == (w["count"], w["prod"])
+            assert g["partitioner_used"] == lib.PART_LEARNED
+    per_replay = counts[2] - counts[1]
+    assert per_replay >= 10 and counts[1] - counts[0] == per_replay
+
+
 def test_batched_1024_windows_hash_equals_sort_merge(lib, oracle):
     """The 1,024-window shape (sizes log-uniform in [2^10, 2^20], keys in [0, 4W)):
     two independent joins agree on every window, and sampled windows equal the oracle."""
