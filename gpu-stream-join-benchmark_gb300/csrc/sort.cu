@@ -3,9 +3,10 @@
 //
 // One pass = three launches over all segments of a batch:
 //   rs_upsweep    per 4096-key tile: digit histogram (one shared atomic per key)
-//   rs_scan       per segment: exclusive scan of its [256 digits x tiles]
-//                 count block, digit-major, so tile t's digit d lands after all
-//                 smaller digits and after digit d of tiles < t (stability)
+//   rs_scan       per segment: each digit's tile counts scanned over the tiles
+//                 (a warp per digit), the digit totals scanned into per-digit
+//                 starts, so tile t's digit d lands after all smaller digits
+//                 and after digit d of tiles < t (stability)
 //   rs_downsweep  per tile: the tile's keys and vals are staged in shared
 //                 memory by TMA bulk copies (cp.async.bulk, mbarrier with a
 //                 bounded wait); stable ranks come from warp-private digit
@@ -194,47 +195,50 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
     counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl] = hist[threadIdx.x];
 }
 
-// One CTA per segment: exclusive scan of its 256 * ntiles counts in place.
+// One CTA per segment.  Each digit's tile counts (contiguous: the block is
+// digit-major) get an exclusive scan over the tiles in place, one warp per
+// digit at a time, 32 tiles per step; the digit totals then get an exclusive
+// scan into digoff[segment][digit].  Tile t's digit d starts at
+// digoff[d] + counts[d][t]: after every smaller digit of the segment and after
+// digit d of the tiles before t (stability).
 __global__ void __launch_bounds__(1024)
-rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs, uint32_t shift,
-               const uint32_t *__restrict__ kmax) {
+rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs, uint32_t *__restrict__ digoff,
+               uint32_t shift, const uint32_t *__restrict__ kmax) {
     if (pass_is_identity(kmax, shift)) return;   // whole grid
-    __shared__ uint32_t warp_tot[32];
-    __shared__ uint32_t carry_s;
+    __shared__ uint32_t dtot[kDigits];
     const SortSeg sg = segs[blockIdx.x];
     uint32_t *c = counts + (uint64_t)sg.tile0 * kDigits;
-    const uint32_t n = kDigits * sg.ntiles;
-    if (threadIdx.x == 0) carry_s = 0;
+    const uint32_t nt = sg.ntiles, lane = lane_id();
+    for (uint32_t d = warp_id(); d < kDigits; d += blockDim.x >> 5) {
+        uint32_t *cd = c + (uint64_t)d * nt;
+        uint32_t carry = 0;
+        for (uint32_t t0 = 0; t0 < nt; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            const uint32_t v = t < nt ? cd[t] : 0u;
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan(v, &tot);
+            if (t < nt) cd[t] = carry + ex;
+            carry += tot;
+        }
+        if (lane == 0) dtot[d] = carry;
+    }
     SJBG_BARRIER();
-    constexpr uint32_t kItems = 4;
-    for (uint32_t base = 0; base < n; base += blockDim.x * kItems) {
-        uint32_t v[kItems], s = 0;
+    if (warp_id() == 0) {
+        constexpr uint32_t kPer = kDigits / 32;
+        uint32_t a[kPer], sum = 0;
 #pragma unroll
-        for (uint32_t k = 0; k < kItems; k++) {
-            const uint32_t i = base + threadIdx.x * kItems + k;
-            v[k] = i < n ? c[i] : 0;
-            s += v[k];
+        for (uint32_t q = 0; q < kPer; q++) {
+            a[q] = dtot[lane * kPer + q];
+            sum += a[q];
         }
-        uint32_t wt;
-        const uint32_t ex = warp_excl_scan(s, &wt);
-        if (lane_id() == 31) warp_tot[warp_id()] = ex + s;
-        SJBG_BARRIER();
-        if (warp_id() == 0) {
-            const uint32_t x = lane_id() < (blockDim.x >> 5) ? warp_tot[lane_id()] : 0;
-            uint32_t tt;
-            warp_tot[lane_id()] = warp_excl_scan(x, &tt);
-        }
-        SJBG_BARRIER();
-        uint32_t run = carry_s + warp_tot[warp_id()] + ex;
+        uint32_t tot;
+        uint32_t run = warp_excl_scan(sum, &tot);
+        uint32_t *dw = digoff + (uint64_t)blockIdx.x * kDigits;
 #pragma unroll
-        for (uint32_t k = 0; k < kItems; k++) {
-            const uint32_t i = base + threadIdx.x * kItems + k;
-            if (i < n) c[i] = run;
-            run += v[k];
+        for (uint32_t q = 0; q < kPer; q++) {
+            dw[lane * kPer + q] = run;
+            run += a[q];
         }
-        SJBG_BARRIER();
-        if (threadIdx.x == blockDim.x - 1) carry_s = run;
-        SJBG_BARRIER();
     }
 }
 
@@ -254,8 +258,8 @@ __global__ void __launch_bounds__(kSortThreads)
 rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
                     const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t shift,
-                    const uint32_t *__restrict__ counts, uint32_t *__restrict__ status,
-                    const uint32_t *__restrict__ kmax) {
+                    const uint32_t *__restrict__ counts, const uint32_t *__restrict__ digoff,
+                    uint32_t *__restrict__ status, const uint32_t *__restrict__ kmax) {
     if (pass_is_identity(kmax, shift)) return;   // whole grid
     extern __shared__ __align__(128) uint8_t smem_raw[];
     DownSmem &sm = *reinterpret_cast<DownSmem *>(smem_raw);
@@ -275,7 +279,8 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
         bulk_g2s(sm.in_vals, vals + sg.off + base, kSortTile * 4, &sm.bar);
     }
     if (threadIdx.x < kDigits)
-        sm.gofs[threadIdx.x] = counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl];
+        sm.gofs[threadIdx.x] = digoff[(uint64_t)s * kDigits + threadIdx.x] +
+                               counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl];
     // every thread waits (bounded); the block leaves together if any gave up
     const bool arrived = mbar_wait(&sm.bar, 0);
     if (!__syncthreads_and(arrived)) {
@@ -450,26 +455,21 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
                         uint32_t *keys2, uint32_t *vals2, uint32_t *status, const SortView **view) {
     const uint32_t nseg = (uint32_t)plan.segs.size();
     uint32_t *dMax = static_cast<uint32_t *>(ws_get(h, WS_STATUS, 64));
-    uint32_t *counts = static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * plan.tiles));
-    uint32_t *hMax = static_cast<uint32_t *>(pinned_get(h, 5, 64));
+    // per tile and digit: the digit's count, then its start among the segment's tiles;
+    // per segment and digit: the digit's start in the segment
+    uint32_t *counts =
+        static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * (plan.tiles + nseg)));
     SortView *dView = static_cast<SortView *>(ws_get(h, WS_SORT_VIEW, sizeof(SortView)));
-    if (!dMax || !counts || !hMax || !dView) return fail(h, SJBG_E_NOMEM, "sort buffers");
+    if (!dMax || !counts || !dView) return fail(h, SJBG_E_NOMEM, "sort buffers");
     SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
     SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
                       plan.tile_seg, dMax));
-    // outside graph capture the key range is read back and only the passes
-    // needed are launched; under capture all four are, and each skips itself
-    // on the device when its digit is zero in every key
-    uint32_t passes = 4;
+    // all four passes are launched and each skips itself on the device when its
+    // digit is zero in every key: no read-back of the key range, no host wait,
+    // and the same launches under graph capture
+    const uint32_t passes = 4;
     const uint32_t *dkmax = dMax;
-    if (!h->capturing) {
-        SJBG_CK(h, cudaMemcpyAsync(hMax, dMax, 8, cudaMemcpyDeviceToHost, h->stream));
-        SJBG_CK(h, cudaStreamSynchronize(h->stream));
-        uint32_t bits = 0;
-        while (bits < 32 && (hMax[0] >> bits)) bits++;
-        passes = (bits + 7) / 8;
-        dkmax = nullptr;
-    }
+    uint32_t *digoff = counts + (size_t)kDigits * plan.tiles;
     const size_t smem = sizeof(DownSmem);
     allow_big_smem(rs_downsweep_kernel, smem);
     uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
@@ -477,10 +477,11 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
         const uint32_t shift = 8 * p;
         SJBG_CK(h, launch(h, "rs_upsweep", rs_upsweep_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)kin,
                           dSegs, plan.tile_seg, shift, counts, dkmax));
-        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs, shift, dkmax));
+        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs, digoff, shift,
+                          dkmax));
         SJBG_CK(h, launch(h, "rs_downsweep", rs_downsweep_kernel, dim3(plan.tiles), dim3(kSortThreads), smem,
                           (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, plan.tile_seg, shift,
-                          (const uint32_t *)counts, status, dkmax));
+                          (const uint32_t *)counts, (const uint32_t *)digoff, status, dkmax));
         std::swap(kin, kout);
         std::swap(vin, vout);
     }

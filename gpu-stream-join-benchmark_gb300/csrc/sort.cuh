@@ -55,9 +55,9 @@ struct SortView {
 
 // Stable LSD sort of every segment by key; keys/vals hold the input, and the
 // result is in keys/vals or keys2/vals2 as *view (a device pointer) says.
-// Outside graph capture the passes are ceil(bits/8) where bits covers the
-// largest key (read back once); under capture each pass skips itself on the
-// device when its digit is zero in every key.
+// Four 8-bit passes are launched; each skips itself on the device when its
+// digit is zero in every key (the largest key is found on the device), so the
+// host never waits and the launches are the same under graph capture.
 // status: a device word that receives kErrTimeout if a tile's bulk copy never lands.
 int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
                         uint32_t *keys2, uint32_t *vals2, uint32_t *status, const SortView **view);
