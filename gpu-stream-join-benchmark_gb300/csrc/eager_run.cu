@@ -17,12 +17,15 @@
 // compared by one grid of register-blocked CTAs (nlj.cu's block routine); a
 // block pair adds its matches to the later batch's count and its checksums to
 // the window.
-// Hash and sort-merge joins: the window totals come from the lazy join of the
-// windows (hj.cu / smj.cu), and the batch counts from one stable sort per
-// window: the window's (key, batch tag) pairs in arrival order are sorted by
-// key (sort.cu), so each key group lists its tuples in arrival order and a
-// tuple's count is the number of other-side tuples before it in its group,
-// which prefix counts over the sorted window give directly.
+// Hash and sort-merge joins: the batch counts come from one stable sort per
+// window: the window's keys in arrival order are sorted (sort.cu) with each
+// tuple's arrival position as payload, so each key group lists its tuples in
+// arrival order and a tuple's count is the number of other-side tuples before
+// it in its group, which a segmented scan over the sorted window gives.
+// Sort-merge without pair enumeration takes the window totals from the same
+// pass (count = the sum of those counts, prod = the same pairs weighted by
+// fr * gs); otherwise they come from the lazy join of the windows (hj.cu /
+// smj.cu).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -34,99 +37,237 @@ namespace sjbg {
 
 // ---------------------------------------------------------------- sort-based batch counts
 constexpr uint32_t kAttrThreads = 256;
-constexpr uint32_t kAttrPer = kSortTile / kAttrThreads;   // 16
+constexpr uint32_t kAttrPer = kSortTile / kAttrThreads;   // 16 consecutive positions per thread
 constexpr uint32_t kTagSmem = 4096;                       // batch counters kept in shared memory
-// dynamic shared memory of eattr_kernel: keys, right prefix, group starts, batch counters
-constexpr size_t kAttrSmem = 3 * sizeof(uint32_t) * kSortTile + sizeof(unsigned long long) * kTagSmem;
 
-// Per window: the batch-counter range its tags fall in.
+// Per window (one sort segment).
 struct ESegMeta {
-    uint32_t tag_lo, tag_n;
+    uint32_t tag_lo, tag_n;   // the batch-counter range its tags fall in
+    uint32_t first_tag;       // arrival tag (2 * batch + side) of the window's first batch
+    uint32_t pad_;
 };
 
-// One copy item: batch `batch` of side `side` -> positions [dst, dst + B) of the window's segment.
+// One copy item: batch `batch` of side `side` -> buffer positions [dst, dst + B),
+// which are positions [rel, rel + B) of its window's segment.
 struct EGather {
     uint64_t dst;
-    uint32_t batch, side;
+    uint32_t batch, side, rel, pad_;
 };
+
+// The sort's payload is a tuple's position in its window's arrival-ordered
+// segment.  A window holds consecutive arrival tags (the close rule is checked
+// before every batch, in arrival order), so the position names the tuple:
+// tag = the window's first tag + position / B, index in the batch = position % B.
+struct ETup {
+    uint32_t tag, val;
+};
+
+__device__ __forceinline__ ETup etuple(uint32_t rel, uint32_t first_tag, const sjbg_tuple *__restrict__ L,
+                                       const sjbg_tuple *__restrict__ R, uint32_t B, bool need_val) {
+    const uint32_t slot = rel / B;
+    const uint32_t tag = first_tag + slot;
+    uint32_t v = 0;
+    if (need_val) {
+        const sjbg_tuple *src = (tag & 1u) ? R : L;
+        v = __ldg(&src[(uint64_t)(tag >> 1) * B + (rel - slot * B)].val);
+    }
+    return ETup{tag, v};
+}
 
 __global__ void __launch_bounds__(256)
 egather_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const EGather *__restrict__ items,
-               uint32_t B, uint32_t *__restrict__ keys, uint32_t *__restrict__ tags) {
+               uint32_t B, uint32_t *__restrict__ keys, uint32_t *__restrict__ rels) {
     const EGather it = items[blockIdx.x];
     const sjbg_tuple *src = (it.side ? R : L) + (uint64_t)it.batch * B;
-    const uint32_t tag = 2u * it.batch + it.side;
     for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) {
         keys[it.dst + i] = __ldg(reinterpret_cast<const uint32_t *>(src + i));
-        tags[it.dst + i] = tag;
+        rels[it.dst + i] = it.rel + i;
     }
 }
 
-// Right-side tuples per sort tile.
+// Sums over a run of a window's sorted tuples: left and right tuples, and the
+// sums of fr over the left ones and of gs over the right ones (the weights
+// exist only when the window's totals are formed here, kW).
+struct ESum {
+    uint32_t nl, nr;
+    unsigned long long wl, wr;
+};
+
+__device__ __forceinline__ ESum esum_zero() { return ESum{0u, 0u, 0ull, 0ull}; }
+
+__device__ __forceinline__ void esum_add(ESum &a, const ESum &b) {
+    a.nl += b.nl;
+    a.nr += b.nr;
+    a.wl += b.wl;
+    a.wr += b.wr;
+}
+
+template <bool kW>
+__device__ __forceinline__ void esum_item(ESum &a, const ETup &e) {
+    if (e.tag & 1u) {
+        a.nr++;
+        if (kW) a.wr += sjbg_gs(e.val);
+    } else {
+        a.nl++;
+        if (kW) a.wl += sjbg_fr(e.val);
+    }
+}
+
+template <bool kW>
+__device__ __forceinline__ ESum esum_shfl_up(const ESum &a, uint32_t o) {
+    ESum y = esum_zero();
+    y.nl = __shfl_up_sync(0xFFFFFFFFu, a.nl, o);
+    y.nr = __shfl_up_sync(0xFFFFFFFFu, a.nr, o);
+    if (kW) {
+        y.wl = __shfl_up_sync(0xFFFFFFFFu, a.wl, o);
+        y.wr = __shfl_up_sync(0xFFFFFFFFu, a.wr, o);
+    }
+    return y;
+}
+
+template <bool kW>
+__device__ __forceinline__ ESum esum_warp_sum(ESum a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a.nl += __shfl_xor_sync(0xFFFFFFFFu, a.nl, o);
+        a.nr += __shfl_xor_sync(0xFFFFFFFFu, a.nr, o);
+        if (kW) {
+            a.wl += __shfl_xor_sync(0xFFFFFFFFu, a.wl, o);
+            a.wr += __shfl_xor_sync(0xFFFFFFFFu, a.wr, o);
+        }
+    }
+    return a;
+}
+
+// A sort tile's sums, then (in place) their exclusive prefix within the segment.
+struct ETileSum {
+    unsigned long long nl, nr, wl, wr;
+};
+
+template <bool kW>
 __global__ void __launch_bounds__(256)
-etile_count_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
-                   const uint32_t *__restrict__ tile_seg, uint32_t *__restrict__ tcount) {
-    const uint32_t *__restrict__ tags = view->vals;
+etile_sum_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
+                 const uint32_t *__restrict__ tile_seg, const ESegMeta *__restrict__ meta,
+                 const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, uint32_t B,
+                 ETileSum *__restrict__ tsum) {
+    const uint32_t *__restrict__ rels = view->vals;
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
+    const uint32_t first = meta[s].first_tag;
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
-    uint32_t c = 0;
-    for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x)
-        if (base + i < sg.n) c += tags[sg.off + base + i] & 1u;
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
-    __shared__ uint32_t part[8];
-    if (lane_id() == 0) part[warp_id()] = c;
+    ESum a = esum_zero();
+    for (uint32_t i = threadIdx.x; i < kSortTile && base + i < sg.n; i += blockDim.x)
+        esum_item<kW>(a, etuple(rels[sg.off + base + i], first, L, R, B, kW));
+    a = esum_warp_sum<kW>(a);
+    __shared__ ESum part[8];
+    if (lane_id() == 0) part[warp_id()] = a;
     SJBG_BARRIER();
     if (threadIdx.x == 0) {
-        uint32_t t = 0;
-        for (uint32_t q = 0; q < blockDim.x / 32; q++) t += part[q];
-        tcount[blockIdx.x] = t;
+        ESum t = esum_zero();
+        for (uint32_t q = 0; q < blockDim.x / 32; q++) esum_add(t, part[q]);
+        tsum[blockIdx.x] = ETileSum{t.nl, t.nr, t.wl, t.wr};
     }
 }
 
-// One warp per segment: exclusive scan of its tiles' right counts.
-__global__ void etile_scan_kernel(const SortSeg *__restrict__ segs, uint32_t nseg, const uint32_t *__restrict__ tcount,
-                                  uint32_t *__restrict__ tpre) {
+// One warp per segment: its tiles' sums become their exclusive prefix.
+__global__ void etile_scan_kernel(const SortSeg *__restrict__ segs, uint32_t nseg, ETileSum *__restrict__ t) {
     const uint32_t s = blockIdx.x;
     if (s >= nseg) return;
     const SortSeg sg = segs[s];
-    uint32_t carry = 0;
+    unsigned long long carry[4] = {0, 0, 0, 0};
     for (uint32_t t0 = 0; t0 < sg.ntiles; t0 += 32) {
-        const uint32_t t = t0 + lane_id();
-        const uint32_t v = t < sg.ntiles ? tcount[sg.tile0 + t] : 0u;
-        uint32_t tot;
-        const uint32_t ex = warp_excl_scan(v, &tot);
-        if (t < sg.ntiles) tpre[sg.tile0 + t] = carry + ex;
-        carry += tot;
+        const uint32_t i = t0 + lane_id();
+        const ETileSum v = i < sg.ntiles ? t[sg.tile0 + i] : ETileSum{0, 0, 0, 0};
+        unsigned long long x[4] = {v.nl, v.nr, v.wl, v.wr}, y[4];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const unsigned long long u = __shfl_up_sync(0xFFFFFFFFu, x[f], o);
+                if (lane_id() >= (uint32_t)o) x[f] += u;
+            }
+#pragma unroll
+        for (int f = 0; f < 4; f++) y[f] = __shfl_sync(0xFFFFFFFFu, x[f], 31);
+        if (i < sg.ntiles)
+            t[sg.tile0 + i] = ETileSum{carry[0] + x[0] - v.nl, carry[1] + x[1] - v.nr, carry[2] + x[2] - v.wl,
+                                       carry[3] + x[3] - v.wr};
+#pragma unroll
+        for (int f = 0; f < 4; f++) carry[f] += y[f];
     }
 }
 
-// Number of right-side tuples at segment positions [0, p): the tile prefix plus
-// the right tuples of p's tile before p (one warp counts them).
-__device__ __forceinline__ uint32_t eright_before_warp(const uint32_t *tags, const SortSeg &sg, const uint32_t *tpre,
-                                                       uint32_t p) {
-    const uint32_t t = p / kSortTile, t0 = t * kSortTile;
-    uint32_t c = 0;
-    for (uint32_t i = t0 + lane_id(); i < p; i += 32) c += tags[sg.off + i] & 1u;
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
-    return tpre[sg.tile0 + t] + c;
+// Sums over the part of a tile's first key group that lies before the tile
+// (zero when the tile starts a group).  Called by one whole warp.  The group
+// start is looked for among the 32 positions before the tile first; a longer
+// group is found by binary search and summed from the tile prefix of the tile
+// it starts in, counting from the nearer end of that tile.
+template <bool kW>
+__device__ ESum efirst_group_carry(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ rels,
+                                   const SortSeg &sg, uint32_t first_tag, const ETileSum *__restrict__ tpre,
+                                   uint32_t tile, uint32_t base, const sjbg_tuple *__restrict__ L,
+                                   const sjbg_tuple *__restrict__ R, uint32_t B) {
+    ESum c = esum_zero();
+    if (base == 0) return c;
+    const uint32_t *__restrict__ ks = keys + sg.off;
+    const uint32_t *__restrict__ rs = rels + sg.off;
+    const uint32_t k0 = ks[base];
+    if (ks[base - 1] != k0) return c;
+    const uint32_t lane = lane_id();
+    const bool in = lane < base && ks[base - 1 - lane] == k0;
+    const uint32_t out = __ballot_sync(0xFFFFFFFFu, !in);
+    if (out) {
+        const uint32_t len = __ffs(out) - 1;   // group positions before the tile
+        if (lane < len) esum_item<kW>(c, etuple(rs[base - 1 - lane], first_tag, L, R, B, kW));
+        return esum_warp_sum<kW>(c);
+    }
+    uint32_t lo = 0, hi = base - 32;   // first position whose key is >= k0
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (ks[mid] < k0) lo = mid + 1; else hi = mid;
+    }
+    const uint32_t g0 = lo, t0 = g0 / kSortTile, a0 = t0 * kSortTile;
+    const bool fwd = g0 - a0 <= a0 + kSortTile - g0;
+    const uint32_t i0 = fwd ? a0 : g0, i1 = fwd ? g0 : a0 + kSortTile;   // inside tile t0, all valid
+    ESum part = esum_zero();
+    for (uint32_t i = i0 + lane; i < i1; i += 32) esum_item<kW>(part, etuple(rs[i], first_tag, L, R, B, kW));
+    part = esum_warp_sum<kW>(part);
+    const ETileSum at = tpre[sg.tile0 + t0 + (fwd ? 0u : 1u)];   // sums before tile t0 (or t0 + 1 <= this tile)
+    const ETileSum cur = tpre[tile];                              // sums before this tile
+    // group part before the tile = S(base) - S(g0), S(g0) = at + part (forward) or at - part
+    c.nl = (uint32_t)(cur.nl - at.nl);
+    c.nr = (uint32_t)(cur.nr - at.nr);
+    c.wl = cur.wl - at.wl;
+    c.wr = cur.wr - at.wr;
+    if (fwd) {
+        c.nl -= part.nl;
+        c.nr -= part.nr;
+        c.wl -= part.wl;
+        c.wr -= part.wr;
+    } else {
+        esum_add(c, part);
+    }
+    return c;
 }
 
 // Per sort tile: each tuple's count = other-side tuples before it in its key
-// group, summed into its batch's counter.
+// group, summed into its batch's counter.  Running sums over the key groups
+// come from a segmented scan of the tile (per thread over its 16 positions,
+// then over threads and warps), continued from the group's part in earlier
+// tiles.  With kW the tile also adds the window's totals: count = all those
+// counts (each pair is counted once, by its later tuple), prod = the same
+// pairs weighted by fr(left) * gs(right).
+template <bool kW>
 __global__ void __launch_bounds__(kAttrThreads)
 eattr_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs,
-             const uint32_t *__restrict__ tile_seg, const ESegMeta *__restrict__ meta, const uint32_t *__restrict__ tpre,
-             unsigned long long *__restrict__ counts) {
-    extern __shared__ __align__(16) uint8_t attr_smem[];
-    unsigned long long *tc = reinterpret_cast<unsigned long long *>(attr_smem);   // kTagSmem batch counters
-    uint32_t *sk = reinterpret_cast<uint32_t *>(tc + kTagSmem);                   // the tile's keys
-    uint32_t *rloc = sk + kSortTile;        // right tuples before each position inside the tile
-    int32_t *gst = reinterpret_cast<int32_t *>(rloc + kSortTile);                  // group start inside the tile, or -1
-    __shared__ uint32_t warp_tot[kAttrThreads / 32];
-    __shared__ uint32_t g0_s, r0_s;
-    const uint32_t *__restrict__ keys = view->keys;   // the sorted keys and their tags
-    const uint32_t *__restrict__ tags = view->vals;
+             const uint32_t *__restrict__ tile_seg, const ESegMeta *__restrict__ meta,
+             const ETileSum *__restrict__ tpre, const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R,
+             uint32_t B, unsigned long long *__restrict__ counts, WinAcc *__restrict__ acc) {
+    __shared__ unsigned long long tc[kTagSmem];   // batch counters of the window
+    __shared__ uint32_t wflag[kAttrThreads / 32];
+    __shared__ ESum wsum[kAttrThreads / 32];
+    __shared__ ESum carry0;
+    const uint32_t *__restrict__ keys = view->keys;   // the sorted keys and their positions
+    const uint32_t *__restrict__ rels = view->vals;
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const ESegMeta m = meta[s];
@@ -136,98 +277,108 @@ eattr_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ segs
     const bool smem_tags = m.tag_n <= kTagSmem;
     if (smem_tags)
         for (uint32_t i = threadIdx.x; i < m.tag_n; i += blockDim.x) tc[i] = 0;
-    // thread t owns positions [t * kAttrPer, (t + 1) * kAttrPer) of the tile
+    // thread t owns positions [t * 16, t * 16 + 16) of the tile; segments start on
+    // tile boundaries, so a full run is four aligned 16-byte loads per array
     const uint32_t p0 = threadIdx.x * kAttrPer;
-    uint32_t myr = 0, tg[kAttrPer];
+    const uint64_t g = sg.off + base + p0;
+    uint32_t k[kAttrPer], tg[kAttrPer], vl[kAttrPer];
+    if (p0 + kAttrPer <= n) {
 #pragma unroll
-    for (int q = 0; q < (int)kAttrPer; q++) {
-        const uint32_t p = p0 + q;
-        const bool valid = p < n;
-        const uint32_t k = valid ? keys[sg.off + base + p] : 0xFFFFFFFFu;
-        tg[q] = valid ? tags[sg.off + base + p] : 0u;
-        sk[p] = k;
-        myr += valid ? (tg[q] & 1u) : 0u;
-    }
-    uint32_t tot;
-    const uint32_t ex = warp_excl_scan(myr, &tot);
-    if (lane_id() == 31) warp_tot[warp_id()] = ex + myr;
-    SJBG_BARRIER();
-    if (warp_id() == 0) {
-        const uint32_t x = lane_id() < blockDim.x / 32 ? warp_tot[lane_id()] : 0u;
-        uint32_t tt;
-        const uint32_t e = warp_excl_scan(x, &tt);   // all 32 lanes
-        if (lane_id() < blockDim.x / 32) warp_tot[lane_id()] = e;
-    }
-    SJBG_BARRIER();
-    uint32_t run = warp_tot[warp_id()] + ex;
-    int32_t last = -1;
-#pragma unroll
-    for (int q = 0; q < (int)kAttrPer; q++) {
-        const uint32_t p = p0 + q;
-        rloc[p] = run;
-        run += (p < n) ? (tg[q] & 1u) : 0u;
-        // a group starts at p when the previous position (this tile or the one before) holds another key
-        const uint32_t prevk = p ? sk[p - 1] : (base ? keys[sg.off + base - 1] : ~sk[0]);
-        const bool head = p < n && (base + p == 0 || prevk != sk[p]);
-        if (head) last = (int32_t)p;
-        gst[p] = last;   // partial: only this thread's run so far
-    }
-    // block-wide max-scan of group starts: carry the last start of earlier threads
-    {
-        int32_t mine = last, incl = mine;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane_id() >= (uint32_t)o) incl = max(incl, y);
+        for (int q = 0; q < (int)kAttrPer; q += 4) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(keys + g + q);
+            const uint4 b = *reinterpret_cast<const uint4 *>(rels + g + q);
+            k[q] = a.x; k[q + 1] = a.y; k[q + 2] = a.z; k[q + 3] = a.w;
+            tg[q] = b.x; tg[q + 1] = b.y; tg[q + 2] = b.z; tg[q + 3] = b.w;
         }
-        __shared__ int32_t wmax[kAttrThreads / 32];
-        if (lane_id() == 31) wmax[warp_id()] = incl;
-        SJBG_BARRIER();
-        int32_t carry = -1;
-        for (uint32_t q = 0; q < warp_id(); q++) carry = max(carry, wmax[q]);
-        int32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1);
-        if (lane_id() == 0) before = -1;
-        before = max(before, carry);
+    } else {
 #pragma unroll
         for (int q = 0; q < (int)kAttrPer; q++) {
-            const uint32_t p = p0 + q;
-            if (gst[p] < 0) gst[p] = before;
+            const bool valid = p0 + q < n;
+            k[q] = valid ? keys[g + q] : 0u;
+            tg[q] = valid ? rels[g + q] : 0u;
         }
     }
-    // the tile's first group may have started in an earlier tile: find its start
-    if (threadIdx.x == 0) g0_s = 0xFFFFFFFFu;
-    SJBG_BARRIER();
-    if (warp_id() == 0 && gst[0] < 0) {
-        const uint32_t k0 = sk[0];
-        uint32_t lo = 0, hi = base;   // first position in [0, base] whose key is >= k0
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (keys[sg.off + mid] < k0) lo = mid + 1; else hi = mid;
-        }
-        const uint32_t r = eright_before_warp(tags, sg, tpre, lo);
-        if (lane_id() == 0) { g0_s = lo; r0_s = r; }
-    }
-    SJBG_BARRIER();
-    const uint32_t tile_r = tpre[blockIdx.x];
+    const uint32_t prev = p0 < n ? (base + p0 ? keys[g - 1] : ~k[0]) : 0u;
+    // pass 1: group heads, and this thread's sums since its last head
+    uint32_t heads = 0, anyh = 0;
+    ESum run = esum_zero();
 #pragma unroll
     for (int q = 0; q < (int)kAttrPer; q++) {
-        const uint32_t p = p0 + q;
-        if (p >= n) break;
-        const uint32_t gp = base + p;   // segment position
-        uint32_t gs, rg;
-        if (gst[p] >= 0) {
-            gs = base + (uint32_t)gst[p];
-            rg = tile_r + rloc[gst[p]];
-        } else {
-            gs = g0_s;
-            rg = r0_s;
+        vl[q] = 0;
+        if (p0 + q < n) {
+            const ETup e = etuple(tg[q], m.first_tag, L, R, B, kW);
+            tg[q] = e.tag;
+            vl[q] = e.val;
+            if (k[q] != (q ? k[q - 1] : prev)) {
+                heads |= 1u << q;
+                run = esum_zero();
+                anyh = 1;
+            }
+            esum_item<kW>(run, e);
         }
-        const uint32_t r_before = tile_r + rloc[p] - rg;            // right tuples before p in its group
-        const uint32_t l_before = (gp - gs) - r_before;              // left tuples before p in its group
-        const uint32_t c = (tg[q] & 1u) ? l_before : r_before;
-        if (!c) continue;
-        if (smem_tags) atomicAdd(&tc[tg[q] - m.tag_lo], (unsigned long long)c);
-        else atomicAdd(&counts[tg[q]], (unsigned long long)c);
     }
+    // segmented scan over the threads: (flag, sums) (+) (flag', sums') =
+    // (flag | flag', flag' ? sums' : sums + sums')
+    uint32_t f = anyh;
+    ESum a = run;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t fy = __shfl_up_sync(0xFFFFFFFFu, f, o);
+        const ESum y = esum_shfl_up<kW>(a, o);
+        if (lane_id() >= o) {
+            if (!f) esum_add(a, y);
+            f |= fy;
+        }
+    }
+    uint32_t ef = __shfl_up_sync(0xFFFFFFFFu, f, 1);
+    ESum ea = esum_shfl_up<kW>(a, 1);
+    if (lane_id() == 0) {
+        ef = 0;
+        ea = esum_zero();
+    }
+    if (lane_id() == 31) {
+        wflag[warp_id()] = f;
+        wsum[warp_id()] = a;
+    }
+    if (warp_id() == 0) {
+        const ESum c = efirst_group_carry<kW>(keys, rels, sg, m.first_tag, tpre, blockIdx.x, base, L, R, B);
+        if (lane_id() == 0) carry0 = c;
+    }
+    SJBG_BARRIER();
+    uint32_t cf = 0;
+    ESum r = esum_zero();
+    for (uint32_t q = 0; q < warp_id(); q++) {
+        if (wflag[q]) {
+            r = wsum[q];
+            cf = 1;
+        } else {
+            esum_add(r, wsum[q]);
+        }
+    }
+    if (ef) r = ea; else esum_add(r, ea);
+    if (!(cf | ef)) esum_add(r, carry0);   // the thread's first group began before the tile
+    // pass 2: counts and weighted pairs against the group's earlier tuples
+    unsigned long long cnt = 0, prod = 0;
+#pragma unroll
+    for (int q = 0; q < (int)kAttrPer; q++) {
+        if (p0 + q < n) {
+            if ((heads >> q) & 1u) r = esum_zero();
+            const bool right = tg[q] & 1u;
+            const uint32_t c = right ? r.nl : r.nr;
+            if (kW) {
+                const unsigned long long w = right ? sjbg_gs(vl[q]) : sjbg_fr(vl[q]);
+                prod += w * (right ? r.wl : r.wr);
+                if (right) r.wr += w; else r.wl += w;
+            }
+            if (right) r.nr++; else r.nl++;
+            cnt += c;
+            if (c) {
+                if (smem_tags) atomicAdd(&tc[tg[q] - m.tag_lo], (unsigned long long)c);
+                else atomicAdd(&counts[tg[q]], (unsigned long long)c);
+            }
+        }
+    }
+    if (kW) flush_acc(&acc[s], cnt, 0ull, prod);
     if (smem_tags) {
         SJBG_BARRIER();
         for (uint32_t i = threadIdx.x; i < m.tag_n; i += blockDim.x)
@@ -309,11 +460,17 @@ int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr
     for (uint32_t w = 0; w < nw; w++) {
         const ERunWin &x = ew[w];
         const uint64_t lo = std::min(x.l0, x.r0), hi = std::max(x.l1, x.r1);
-        meta[w] = ESegMeta{(uint32_t)(2 * lo), (uint32_t)(2 * (hi - lo))};
-        uint64_t pos = plan.segs[w].off;
+        // a window opens with left batch l0 (r0 == l0) or with right batch r0 (l0 == r0 + 1)
+        const uint32_t first = x.l0 <= x.r0 ? (uint32_t)(2 * x.l0) : (uint32_t)(2 * x.r0 + 1);
+        meta[w] = ESegMeta{(uint32_t)(2 * lo), (uint32_t)(2 * (hi - lo)), first, 0};
+        const uint64_t off = plan.segs[w].off;
+        uint64_t pos = off;
         for (uint64_t b = lo; b < hi; b++) {   // arrival order: left batch b, then right batch b
-            if (b >= x.l0 && b < x.l1) { gat.push_back(EGather{pos, (uint32_t)b, 0}); pos += B; }
-            if (b >= x.r0 && b < x.r1) { gat.push_back(EGather{pos, (uint32_t)b, 1}); pos += B; }
+            for (uint32_t side = 0; side < 2; side++) {
+                if (b < (side ? x.r0 : x.l0) || b >= (side ? x.r1 : x.l1)) continue;
+                gat.push_back(EGather{pos, (uint32_t)b, side, (uint32_t)(pos - off), 0});
+                pos += B;
+            }
         }
     }
     const size_t segB = sizeof(SortSeg) * nw, metaB = sizeof(ESegMeta) * nw, gatB = sizeof(EGather) * gat.size();
@@ -324,8 +481,8 @@ int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr
     uint32_t *t0 = static_cast<uint32_t *>(ws_get(h, WS_EAGER_V0, sizeof(uint32_t) * plan.elems));
     uint32_t *k1 = static_cast<uint32_t *>(ws_get(h, WS_EAGER_K1, sizeof(uint32_t) * plan.elems));
     uint32_t *t1 = static_cast<uint32_t *>(ws_get(h, WS_EAGER_V1, sizeof(uint32_t) * plan.elems));
-    uint32_t *tcnt = static_cast<uint32_t *>(ws_get(h, WS_EAGER_TILES, sizeof(uint32_t) * 2 * std::max(plan.tiles, 1u)));
-    if (!hst || !dev || !k0 || !t0 || !k1 || !t1 || !tcnt) return fail(h, SJBG_E_NOMEM, "eager run buffers");
+    ETileSum *tpre = static_cast<ETileSum *>(ws_get(h, WS_EAGER_TILES, sizeof(ETileSum) * std::max(plan.tiles, 1u)));
+    if (!hst || !dev || !k0 || !t0 || !k1 || !t1 || !tpre) return fail(h, SJBG_E_NOMEM, "eager run buffers");
     std::memcpy(hst, plan.segs.data(), segB);
     std::memcpy(hst + segB, meta.data(), metaB);
     std::memcpy(hst + segB + metaB, gat.data(), gatB);
@@ -339,14 +496,25 @@ int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr
     const SortView *view = nullptr;
     int rc = radix_sort_segments(h, plan, dSegs, k0, t0, k1, t1, reinterpret_cast<uint32_t *>(&dWin[nw].info), &view);
     if (rc) return rc;
-    uint32_t *tpre = tcnt + std::max(plan.tiles, 1u);
-    SJBG_CK(h, launch(h, "erun_tile_count", etile_count_kernel, dim3(plan.tiles), dim3(256), 0, view, dSegs,
-                      plan.tile_seg, tcnt));
-    SJBG_CK(h, launch(h, "erun_tile_scan", etile_scan_kernel, dim3(nw), dim3(32), 0, dSegs, nw,
-                      (const uint32_t *)tcnt, tpre));
-    allow_big_smem(eattr_kernel, kAttrSmem);
-    SJBG_CK(h, launch(h, "erun_attribute", eattr_kernel, dim3(plan.tiles), dim3(kAttrThreads), kAttrSmem,
-                      view, dSegs, plan.tile_seg, dMeta, (const uint32_t *)tpre, dCounts));
+    // sort-merge without pair enumeration: the attribution also forms the window
+    // totals (the sorted window is the merge of its two sides); otherwise the
+    // lazy join of the windows forms them
+    const bool totals = h->cfg.algorithm == SJBG_ALG_SMJ && !enumerate;
+    const uint32_t uB = (uint32_t)B;
+    if (totals)
+        SJBG_CK(h, launch(h, "erun_tile_sum", etile_sum_kernel<true>, dim3(plan.tiles), dim3(256), 0, view, dSegs,
+                          plan.tile_seg, dMeta, dl, dr, uB, tpre));
+    else
+        SJBG_CK(h, launch(h, "erun_tile_sum", etile_sum_kernel<false>, dim3(plan.tiles), dim3(256), 0, view, dSegs,
+                          plan.tile_seg, dMeta, dl, dr, uB, tpre));
+    SJBG_CK(h, launch(h, "erun_tile_scan", etile_scan_kernel, dim3(nw), dim3(32), 0, dSegs, nw, tpre));
+    if (totals) {
+        SJBG_CK(h, launch(h, "erun_attribute", eattr_kernel<true>, dim3(plan.tiles), dim3(kAttrThreads), 0, view,
+                          dSegs, plan.tile_seg, dMeta, (const ETileSum *)tpre, dl, dr, uB, dCounts, dWin));
+        return SJBG_OK;
+    }
+    SJBG_CK(h, launch(h, "erun_attribute", eattr_kernel<false>, dim3(plan.tiles), dim3(kAttrThreads), 0, view,
+                      dSegs, plan.tile_seg, dMeta, (const ETileSum *)tpre, dl, dr, uB, dCounts, dWin));
 
     uint32_t pu = 0;
     if (h->cfg.algorithm == SJBG_ALG_SMJ) return smj_lazy_batch(h, dl, dr, wh.data(), nw, nullptr, dWin, enumerate);

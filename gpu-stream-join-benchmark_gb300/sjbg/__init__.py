@@ -262,7 +262,13 @@ class Joiner:
         res = (WindowResult * mw)()
         self._check(self.lib.sjbg_eager_run(self.h, _ptr(left), _ptr(right), n_batches, mem, _ptr(bc),
                                             C.cast(res, C.c_void_p), mw))
-        return bc, [r.as_dict() for r in res]
+        # entries past the stream's last window carry status E_INVALID; only the
+        # windows themselves are converted (a per-entry loop over all 2n + 2 slots
+        # costs milliseconds of host time per call)
+        words = np.frombuffer(res, dtype=np.uint32).reshape(mw, C.sizeof(WindowResult) // 4)
+        absent = np.flatnonzero(words[:, WindowResult.status.offset // 4] == 1)
+        n = int(absent[0]) if absent.size else mw
+        return bc, [res[i].as_dict() for i in range(n)]
 
     # ---- streaming
     def stream_open(self, window_ns: int):

@@ -229,14 +229,18 @@ SJBG_API int sjbg_eager_window_result(sjbg_handle *h, sjbg_pair *pairs, uint64_t
 /* Replaces BaseEagerExecutor::onEndOfStream (BaseEagerExecutor.hpp:20). */
 SJBG_API int sjbg_eager_end_of_stream(sjbg_handle *h);
 
-/* Persistent-kernel form of a whole eager stream: n_batches left batches and
- * n_batches right batches of batch_size tuples, fed in the reference's order
- * L0, R0, L1, R1, ... (src/sjb/source/Source.cpp:20-28) with a window closed
- * whenever either side has received window_size tuples
- * (include/sjb/windowing/eager/CountBased.cuh:38-46).  One launch drains a
- * device work queue of batches.  batch_counts (host, 2*n_batches entries,
- * may be NULL) receives each batch's new matches in arrival order; out
- * (host, one entry per window) receives the window totals. */
+/* A whole recorded eager stream in one call: n_batches left batches and
+ * n_batches right batches of batch_size tuples, with the results of feeding
+ * them in the reference's order L0, R0, L1, R1, ...
+ * (src/sjb/source/Source.cpp:20-28) with a window closed whenever either side
+ * has received window_size tuples
+ * (include/sjb/windowing/eager/CountBased.cuh:38-46).  All windows are joined
+ * together on the device (nested-loop: one grid over every batch pair; hash
+ * and sort-merge: one stable sort per window for the batch counts plus the
+ * lazy join of the windows).  batch_counts (host, 2*n_batches entries, may be
+ * NULL) receives each batch's new matches in arrival order; out (host, one
+ * entry per window) receives the window totals, and entries past the last
+ * window get status SJBG_E_INVALID. */
 SJBG_API int sjbg_eager_run(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *right,
                    uint64_t n_batches, uint32_t mem,
                    uint64_t *batch_counts, sjbg_window_result *out, uint32_t n_windows_out);

@@ -103,6 +103,33 @@ def test_eager_config_shapes(lib, oracle, name, W, D, nb):
         assert (w["xor"], w["prod"]) == (e["xor"], e["prod"])
 
 
+@pytest.mark.parametrize("W,D,nb", [(1 << 20, 1 << 20, 300), (1 << 14, 64, 24), (1 << 14, 3, 12), (5000, 1 << 12, 9),
+                                    (1 << 16, 1 << 30, 33)])
+def test_eager_sort_merge_totals_from_batch_count_pass(lib, oracle, W, D, nb):
+    """Sort-merge without pair enumeration takes each window's count and prod
+    from the pass that forms the batch counts.  Cases: nearly distinct keys;
+    key groups of ~500 tuples and of ~11,000 tuples, which span sort tiles of
+    4,096 (the part of a group before a tile is found by binary search and
+    summed from both ends of its tile); a window of 5,000 with batches of
+    4,096, so that windows open alternately with a left and a right batch;
+    keys that are all distinct."""
+    B = 4096
+    left = oracle.gen_uniform(0, nb * B, 5, D)
+    right = oracle.gen_uniform(0, nb * B, 6, D)
+    want_bc, want_wc = oracle.eager_hj(left, right, B, W, min(D, 1 << 22))
+    with lib.Joiner(lib.ALG_SMJ, lib.EAGER, batch_size=B, window_size=W, max_tuples_per_window=W) as j:
+        bc, wins = j.eager_run(left, right, nb)
+    assert np.array_equal(bc, want_bc)
+    members = window_members(nb, B, W)
+    assert len(wins) == len(members) == len(want_wc)
+    for w, (lb, rb), wc in zip(wins, members, want_wc):
+        l = np.concatenate([left[b * B:(b + 1) * B] for b in lb]) if lb else left[:0]
+        r = np.concatenate([right[b * B:(b + 1) * B] for b in rb]) if rb else right[:0]
+        e = oracle.join(l, r, enumerate_pairs=False)
+        assert (w["count"], w["prod"]) == (e["count"], e["prod"]) and w["count"] == int(wc)
+        assert w["xor"] is None and w["n_pairs"] == 0
+
+
 def test_eager_errors(lib):
     with lib.Joiner(lib.ALG_HJ, lib.LAZY) as j:
         with pytest.raises(lib.SjbgError) as e:
