@@ -76,13 +76,17 @@ __device__ __forceinline__ ETup etuple(uint32_t rel, uint32_t first_tag, const s
 
 __global__ void __launch_bounds__(256)
 egather_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const EGather *__restrict__ items,
-               uint32_t B, uint32_t *__restrict__ keys, uint32_t *__restrict__ rels) {
+               uint32_t B, uint32_t *__restrict__ keys, uint32_t *__restrict__ rels, uint32_t *__restrict__ kmax) {
     const EGather it = items[blockIdx.x];
     const sjbg_tuple *src = (it.side ? R : L) + (uint64_t)it.batch * B;
+    uint32_t m = 0;
     for (uint32_t i = threadIdx.x; i < B; i += blockDim.x) {
-        keys[it.dst + i] = __ldg(reinterpret_cast<const uint32_t *>(src + i));
+        const uint32_t k = __ldg(reinterpret_cast<const uint32_t *>(src + i));
+        keys[it.dst + i] = k;
         rels[it.dst + i] = it.rel + i;
+        m = max(m, k);
     }
+    block_key_max(m, kmax);   // the sort's key range
 }
 
 // Sums over a run of a window's sorted tuples: left and right tuples, and the
@@ -155,9 +159,21 @@ etile_sum_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ 
     const SortSeg sg = segs[s];
     const uint32_t first = meta[s].first_tag;
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
+    // all 16 positions' loads first, then their gathers, then the sums
+    constexpr uint32_t kPer = kSortTile / 256;
+    uint32_t rl[kPer];
+#pragma unroll
+    for (uint32_t q = 0; q < kPer; q++) {
+        const uint32_t i = base + threadIdx.x + q * 256;
+        rl[q] = i < sg.n ? rels[sg.off + i] : 0u;
+    }
+    ETup e[kPer];
+#pragma unroll
+    for (uint32_t q = 0; q < kPer; q++) e[q] = etuple(rl[q], first, L, R, B, kW);
     ESum a = esum_zero();
-    for (uint32_t i = threadIdx.x; i < kSortTile && base + i < sg.n; i += blockDim.x)
-        esum_item<kW>(a, etuple(rels[sg.off + base + i], first, L, R, B, kW));
+#pragma unroll
+    for (uint32_t q = 0; q < kPer; q++)
+        if (base + threadIdx.x + q * 256 < sg.n) esum_item<kW>(a, e[q]);
     a = esum_warp_sum<kW>(a);
     __shared__ ESum part[8];
     if (lane_id() == 0) part[warp_id()] = a;
@@ -169,30 +185,42 @@ etile_sum_kernel(const SortView *__restrict__ view, const SortSeg *__restrict__ 
     }
 }
 
-// One warp per segment: its tiles' sums become their exclusive prefix.
+// One warp per segment: its tiles' sums become their exclusive prefix.  Each
+// lane sums a run of consecutive tiles (independent loads), the lane sums get
+// a warp scan, and each lane writes its run's prefixes.
 __global__ void etile_scan_kernel(const SortSeg *__restrict__ segs, uint32_t nseg, ETileSum *__restrict__ t) {
     const uint32_t s = blockIdx.x;
     if (s >= nseg) return;
     const SortSeg sg = segs[s];
-    unsigned long long carry[4] = {0, 0, 0, 0};
-    for (uint32_t t0 = 0; t0 < sg.ntiles; t0 += 32) {
-        const uint32_t i = t0 + lane_id();
-        const ETileSum v = i < sg.ntiles ? t[sg.tile0 + i] : ETileSum{0, 0, 0, 0};
-        unsigned long long x[4] = {v.nl, v.nr, v.wl, v.wr}, y[4];
+    ETileSum *ts = t + sg.tile0;
+    const uint32_t nt = sg.ntiles, per = (nt + 31) >> 5;
+    const uint32_t a = min(nt, lane_id() * per), b = min(nt, a + per);
+    unsigned long long x[4] = {0, 0, 0, 0};
+    for (uint32_t i = a; i < b; i++) {
+        const ETileSum v = ts[i];
+        x[0] += v.nl;
+        x[1] += v.nr;
+        x[2] += v.wl;
+        x[3] += v.wr;
+    }
+    unsigned long long run[4];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
+    for (int f = 0; f < 4; f++) {
+        unsigned long long inc = x[f];
 #pragma unroll
-            for (int f = 0; f < 4; f++) {
-                const unsigned long long u = __shfl_up_sync(0xFFFFFFFFu, x[f], o);
-                if (lane_id() >= (uint32_t)o) x[f] += u;
-            }
-#pragma unroll
-        for (int f = 0; f < 4; f++) y[f] = __shfl_sync(0xFFFFFFFFu, x[f], 31);
-        if (i < sg.ntiles)
-            t[sg.tile0 + i] = ETileSum{carry[0] + x[0] - v.nl, carry[1] + x[1] - v.nr, carry[2] + x[2] - v.wl,
-                                       carry[3] + x[3] - v.wr};
-#pragma unroll
-        for (int f = 0; f < 4; f++) carry[f] += y[f];
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane_id() >= (uint32_t)o) inc += u;
+        }
+        run[f] = inc - x[f];
+    }
+    for (uint32_t i = a; i < b; i++) {
+        const ETileSum v = ts[i];
+        ts[i] = ETileSum{run[0], run[1], run[2], run[3]};
+        run[0] += v.nl;
+        run[1] += v.nr;
+        run[2] += v.wl;
+        run[3] += v.wr;
     }
 }
 
@@ -491,10 +519,13 @@ int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr
     const ESegMeta *dMeta = reinterpret_cast<const ESegMeta *>(dev + segB);
     const EGather *dGat = reinterpret_cast<const EGather *>(dev + segB + metaB);
     if (int rc_map = sort_tile_map(h, plan, dSegs)) return rc_map;
+    uint32_t *kmax = nullptr;
+    if (int rc_max = sort_key_max(h, &kmax)) return rc_max;
     SJBG_CK(h, launch(h, "erun_gather", egather_kernel, dim3((uint32_t)gat.size()), dim3(256), 0, dl, dr, dGat,
-                      (uint32_t)B, k0, t0));
+                      (uint32_t)B, k0, t0, kmax));
     const SortView *view = nullptr;
-    int rc = radix_sort_segments(h, plan, dSegs, k0, t0, k1, t1, reinterpret_cast<uint32_t *>(&dWin[nw].info), &view);
+    int rc = radix_sort_segments(h, plan, dSegs, k0, t0, k1, t1, reinterpret_cast<uint32_t *>(&dWin[nw].info), &view,
+                                 kmax);
     if (rc) return rc;
     // sort-merge without pair enumeration: the attribution also forms the window
     // totals (the sorted window is the merge of its two sides); otherwise the

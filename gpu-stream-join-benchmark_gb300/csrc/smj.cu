@@ -209,8 +209,12 @@ int smj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, c
     if (int rc_map = sort_tile_map(h, plan, dSegs)) return rc_map;
 
     const SortView *view = nullptr;
-    int rc = sort_extract(h, dL, dR, n, plan, dSegs, k0, v0);
-    if (!rc) rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1, reinterpret_cast<uint32_t *>(&acc[n].info), &view);
+    uint32_t *kmax = nullptr;
+    int rc = sort_key_max(h, &kmax);
+    if (!rc) rc = sort_extract(h, dL, dR, n, plan, dSegs, k0, v0, kmax);
+    if (!rc)
+        rc = radix_sort_segments(h, plan, dSegs, k0, v0, k1, v1, reinterpret_cast<uint32_t *>(&acc[n].info), &view,
+                                 kmax);
     if (!rc) rc = segmented_fr_prefix(h, plan, n, dSegs, view, F);
     if (rc) return rc;
     if (tiles == 0) return SJBG_OK;

@@ -123,11 +123,12 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d) {
 __global__ void __launch_bounds__(256)
 sort_extract_kernel(const sjbg_tuple *__restrict__ srcA, const sjbg_tuple *__restrict__ srcB, uint32_t split,
                     const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t *__restrict__ keys,
-                    uint32_t *__restrict__ vals) {
+                    uint32_t *__restrict__ vals, uint32_t *__restrict__ kmax) {
     const uint32_t s = find_seg(tile_seg, blockIdx.x);
     const SortSeg sg = segs[s];
     const sjbg_tuple *src = s < split ? srcA : srcB;
     const uint32_t base = (blockIdx.x - sg.tile0) * kSortTile;
+    uint32_t m = 0;
     for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x) {
         const uint32_t li = base + i;
         uint32_t k = 0xFFFFFFFFu, v = 0;
@@ -135,10 +136,12 @@ sort_extract_kernel(const sjbg_tuple *__restrict__ srcA, const sjbg_tuple *__res
             const uint2 t = __ldg(reinterpret_cast<const uint2 *>(src + sg.src + li));
             k = t.x;
             v = t.y;
+            m = max(m, k);
         }
         keys[sg.off + li] = k;
         vals[sg.off + li] = v;
     }
+    if (kmax) block_key_max(m, kmax);
 }
 
 __global__ void __launch_bounds__(256)
@@ -150,16 +153,7 @@ sort_max_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__ s
     uint32_t m = 0;
     for (uint32_t i = threadIdx.x; i < kSortTile; i += blockDim.x)
         if (base + i < sg.n) m = max(m, keys[sg.off + base + i]);
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
-    // one atomic per CTA, and only when it can raise the value seen (a stale
-    // read only costs an atomic: atomicMax decides)
-    __shared__ uint32_t wm[8];
-    if (lane_id() == 0) wm[warp_id()] = m;
-    SJBG_BARRIER();
-    if (threadIdx.x == 0) {
-        for (uint32_t q = 1; q < blockDim.x / 32; q++) m = max(m, wm[q]);
-        if (m > *(volatile const uint32_t *)out) atomicMax(out, m);
-    }
+    block_key_max(m, out);
 }
 
 // counts block of segment s: counts[tile0 * 256 + d * ntiles + t_local]
@@ -195,45 +189,75 @@ rs_upsweep_kernel(const uint32_t *__restrict__ keys, const SortSeg *__restrict__
     counts[(uint64_t)sg.tile0 * kDigits + (uint64_t)threadIdx.x * sg.ntiles + tl] = hist[threadIdx.x];
 }
 
-// One CTA per segment.  Each digit's tile counts (contiguous: the block is
-// digit-major) get an exclusive scan over the tiles in place, one warp per
-// digit at a time, 32 tiles per step; the digit totals then get an exclusive
-// scan into digoff[segment][digit].  Tile t's digit d starts at
-// digoff[d] + counts[d][t]: after every smaller digit of the segment and after
-// digit d of the tiles before t (stability).
-__global__ void __launch_bounds__(1024)
+// Grid (segments, G): CTA (s, g) scans digits [g * 256 / G, (g + 1) * 256 / G)
+// of segment s, 256 / (8 G) consecutive digits per warp.  Each digit's tile
+// counts (contiguous: the block is digit-major) get an exclusive scan over the
+// tiles in place.  A warp walks its (digit, 32-tile chunk) items eight at a
+// time, the eight loads issued before the eight scans, so few and many tiles
+// per segment both keep loads in flight.  The digit totals go to dtot; the
+// segment's last CTA to finish (a counter per segment, reset by that CTA for
+// the next pass) scans them into digoff[segment][digit].  Tile t's digit d
+// starts at digoff[d] + counts[d][t]: after every smaller digit of the
+// segment and after digit d of the tiles before t (stability).  Segments hold
+// at least one tile.
+__global__ void __launch_bounds__(256)
 rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs, uint32_t *__restrict__ digoff,
-               uint32_t shift, const uint32_t *__restrict__ kmax) {
+               uint32_t *__restrict__ dtot, uint32_t *__restrict__ done, uint32_t shift,
+               const uint32_t *__restrict__ kmax) {
     if (pass_is_identity(kmax, shift)) return;   // whole grid
-    __shared__ uint32_t dtot[kDigits];
-    const SortSeg sg = segs[blockIdx.x];
+    __shared__ uint32_t last;
+    const uint32_t s = blockIdx.x, G = gridDim.y;
+    const SortSeg sg = segs[s];
     uint32_t *c = counts + (uint64_t)sg.tile0 * kDigits;
     const uint32_t nt = sg.ntiles, lane = lane_id();
-    for (uint32_t d = warp_id(); d < kDigits; d += blockDim.x >> 5) {
-        uint32_t *cd = c + (uint64_t)d * nt;
-        uint32_t carry = 0;
-        for (uint32_t t0 = 0; t0 < nt; t0 += 32) {
-            const uint32_t t = t0 + lane;
-            const uint32_t v = t < nt ? cd[t] : 0u;
-            uint32_t tot;
-            const uint32_t ex = warp_excl_scan(v, &tot);
-            if (t < nt) cd[t] = carry + ex;
-            carry += tot;
+    const uint32_t pw = kDigits / (G * (blockDim.x >> 5));                  // digits per warp
+    const uint32_t d0 = blockIdx.y * (kDigits / G) + warp_id() * pw;        // the warp's first digit
+    const uint32_t nch = (nt + 31) >> 5, items = pw * nch;
+    uint32_t carry = 0;
+    for (uint32_t i0 = 0; i0 < items; i0 += 8) {
+        uint32_t v[8];
+#pragma unroll
+        for (uint32_t j = 0; j < 8; j++) {
+            const uint32_t i = i0 + j, row = i / nch, t = (i - row * nch) * 32 + lane;
+            v[j] = (i < items && t < nt) ? c[(uint64_t)(d0 + row) * nt + t] : 0u;
         }
-        if (lane == 0) dtot[d] = carry;
+#pragma unroll
+        for (uint32_t j = 0; j < 8; j++) {
+            const uint32_t i = i0 + j;
+            if (i >= items) break;   // uniform over the warp
+            const uint32_t row = i / nch, ch = i - row * nch, t = ch * 32 + lane;
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan(v[j], &tot);
+            if (t < nt) c[(uint64_t)(d0 + row) * nt + t] = carry + ex;
+            carry += tot;
+            if (ch == nch - 1) {
+                if (lane == 0) dtot[(uint64_t)s * kDigits + d0 + row] = carry;
+                carry = 0;
+            }
+        }
     }
-    SJBG_BARRIER();
+    if (G > 1) {
+        __threadfence();
+        SJBG_BARRIER();
+        if (threadIdx.x == 0) last = atomicAdd(&done[s], 1u) == G - 1;
+        SJBG_BARRIER();
+        if (!last) return;
+        __threadfence();
+        if (threadIdx.x == 0) done[s] = 0;
+    } else {
+        SJBG_BARRIER();
+    }
     if (warp_id() == 0) {
         constexpr uint32_t kPer = kDigits / 32;
         uint32_t a[kPer], sum = 0;
 #pragma unroll
         for (uint32_t q = 0; q < kPer; q++) {
-            a[q] = dtot[lane * kPer + q];
+            a[q] = __ldcg(&dtot[(uint64_t)s * kDigits + lane * kPer + q]);
             sum += a[q];
         }
         uint32_t tot;
         uint32_t run = warp_excl_scan(sum, &tot);
-        uint32_t *dw = digoff + (uint64_t)blockIdx.x * kDigits;
+        uint32_t *dw = digoff + (uint64_t)s * kDigits;
 #pragma unroll
         for (uint32_t q = 0; q < kPer; q++) {
             dw[lane * kPer + q] = run;
@@ -444,32 +468,48 @@ int sort_tile_map(sjbg_handle *h, SortPlan &plan, const SortSeg *dSegs) {
     return SJBG_OK;
 }
 
+int sort_key_max(sjbg_handle *h, uint32_t **kmax) {
+    *kmax = static_cast<uint32_t *>(ws_get(h, WS_STATUS, 64));
+    if (!*kmax) return fail(h, SJBG_E_NOMEM, "sort buffers");
+    SJBG_CK(h, cudaMemsetAsync(*kmax, 0, 64, h->stream));
+    return SJBG_OK;
+}
+
 int sort_extract(sjbg_handle *h, const sjbg_tuple *srcA, const sjbg_tuple *srcB, uint32_t split, const SortPlan &plan,
-                 const SortSeg *dSegs, uint32_t *keys, uint32_t *vals) {
+                 const SortSeg *dSegs, uint32_t *keys, uint32_t *vals, uint32_t *kmax) {
     SJBG_CK(h, launch(h, "sort_extract", sort_extract_kernel, dim3(plan.tiles), dim3(256), 0, srcA, srcB, split, dSegs,
-                      plan.tile_seg, keys, vals));
+                      plan.tile_seg, keys, vals, kmax));
     return SJBG_OK;
 }
 
 int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSegs, uint32_t *keys, uint32_t *vals,
-                        uint32_t *keys2, uint32_t *vals2, uint32_t *status, const SortView **view) {
+                        uint32_t *keys2, uint32_t *vals2, uint32_t *status, const SortView **view, uint32_t *kmax) {
     const uint32_t nseg = (uint32_t)plan.segs.size();
-    uint32_t *dMax = static_cast<uint32_t *>(ws_get(h, WS_STATUS, 64));
+    uint32_t *dMax = kmax;
+    if (!dMax)
+        if (int rc = sort_key_max(h, &dMax)) return rc;
     // per tile and digit: the digit's count, then its start among the segment's tiles;
     // per segment and digit: the digit's start in the segment
+    // then per segment and digit the digit's total, and per segment a finished-CTA counter
     uint32_t *counts =
-        static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * kDigits * (plan.tiles + nseg)));
+        static_cast<uint32_t *>(ws_get(h, WS_SORT_HIST, sizeof(uint32_t) * (kDigits * (plan.tiles + 2 * nseg) + nseg)));
     SortView *dView = static_cast<SortView *>(ws_get(h, WS_SORT_VIEW, sizeof(SortView)));
-    if (!dMax || !counts || !dView) return fail(h, SJBG_E_NOMEM, "sort buffers");
-    SJBG_CK(h, cudaMemsetAsync(dMax, 0, 64, h->stream));
-    SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
-                      plan.tile_seg, dMax));
+    if (!counts || !dView) return fail(h, SJBG_E_NOMEM, "sort buffers");
+    if (!kmax)
+        SJBG_CK(h, launch(h, "sort_max", sort_max_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)keys, dSegs,
+                          plan.tile_seg, dMax));
     // all four passes are launched and each skips itself on the device when its
     // digit is zero in every key: no read-back of the key range, no host wait,
     // and the same launches under graph capture
     const uint32_t passes = 4;
     const uint32_t *dkmax = dMax;
     uint32_t *digoff = counts + (size_t)kDigits * plan.tiles;
+    uint32_t *dtot = digoff + (size_t)kDigits * nseg;
+    uint32_t *done = dtot + (size_t)kDigits * nseg;
+    SJBG_CK(h, cudaMemsetAsync(done, 0, sizeof(uint32_t) * nseg, h->stream));
+    // CTAs per segment: as many as keep the scan within about one wave of 256-thread CTAs
+    uint32_t G = 1;
+    while (G < 32 && (uint64_t)nseg * G * 2 <= 1216) G *= 2;
     const size_t smem = sizeof(DownSmem);
     allow_big_smem(rs_downsweep_kernel, smem);
     uint32_t *kin = keys, *vin = vals, *kout = keys2, *vout = vals2;
@@ -477,8 +517,8 @@ int radix_sort_segments(sjbg_handle *h, const SortPlan &plan, const SortSeg *dSe
         const uint32_t shift = 8 * p;
         SJBG_CK(h, launch(h, "rs_upsweep", rs_upsweep_kernel, dim3(plan.tiles), dim3(256), 0, (const uint32_t *)kin,
                           dSegs, plan.tile_seg, shift, counts, dkmax));
-        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg), dim3(1024), 0, counts, dSegs, digoff, shift,
-                          dkmax));
+        SJBG_CK(h, launch(h, "rs_scan", rs_scan_kernel, dim3(nseg, G), dim3(256), 0, counts, dSegs, digoff, dtot, done,
+                          shift, dkmax));
         SJBG_CK(h, launch(h, "rs_downsweep", rs_downsweep_kernel, dim3(plan.tiles), dim3(kSortThreads), smem,
                           (const uint32_t *)kin, (const uint32_t *)vin, kout, vout, dSegs, plan.tile_seg, shift,
                           (const uint32_t *)counts, (const uint32_t *)digoff, status, dkmax));
