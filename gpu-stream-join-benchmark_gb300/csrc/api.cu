@@ -56,7 +56,7 @@ int cuda_fail(sjbg_handle *h, cudaError_t e, const char *what) {
 
 void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes) {
     DevBuf &b = h->ws[s];
-    if (bytes == 0) bytes = 16;
+    bytes = std::max<size_t>(16, (bytes + 15) & ~(size_t)15);   // whole 16-byte words (stage_copy, zero_fill)
     if (b.bytes >= bytes) return b.p;
     if (b.p) {
         cudaStreamSynchronize(h->stream);   // a kernel may still use the old buffer
@@ -80,7 +80,7 @@ void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes) {
 
 void *pinned_get(sjbg_handle *h, int i, size_t bytes) {
     DevBuf &b = h->pinned[i];
-    if (bytes == 0) bytes = 16;
+    bytes = std::max<size_t>(16, (bytes + 15) & ~(size_t)15);
     if (b.bytes >= bytes) return b.p;
     if (b.p) {
         cudaStreamSynchronize(h->stream);
@@ -102,13 +102,31 @@ void *pinned_get(sjbg_handle *h, int i, size_t bytes) {
 // and device memory are done by a kernel over mapped pinned memory, not by a
 // copy engine: a copy engine works its queue in order, so a plan upload
 // queued behind a large input copy on another stream would wait for it.
+// Both buffers come from ws_get / pinned_get, whose sizes are whole 16-byte
+// words, so a 16-byte-aligned pair is copied in whole words: one round of
+// loads over the host link, no byte tail.
 __global__ void stage_copy_kernel(uint8_t *__restrict__ dst, const uint8_t *__restrict__ src, size_t bytes,
                                   bool vec) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    const size_t n16 = vec ? bytes / 16 : 0;
+    const size_t n16 = vec ? (bytes + 15) / 16 : 0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += stride)
         reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
-    for (size_t i = n16 * 16 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < bytes; i += stride) dst[i] = src[i];
+    if (vec) return;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < bytes; i += stride) dst[i] = src[i];
+}
+
+__global__ void zero_fill_kernel(uint4 *__restrict__ dst, size_t n16) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = make_uint4(0, 0, 0, 0);
+}
+
+int zero_fill(sjbg_handle *h, void *dst, size_t bytes) {
+    const size_t n16 = (bytes + 15) / 16;
+    if (n16 == 0) return SJBG_OK;
+    const uint32_t blocks =
+        (uint32_t)std::min<size_t>((n16 + 255) / 256, (size_t)8 * (size_t)std::max(h->num_sms, 1));
+    SJBG_CK(h, launch(h, "zero_fill", zero_fill_kernel, dim3(blocks), dim3(256), 0, static_cast<uint4 *>(dst), n16));
+    return SJBG_OK;
 }
 
 int stage_copy(sjbg_handle *h, void *dst, const void *src, size_t bytes) {

@@ -293,7 +293,7 @@ int hj_global_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     std::memcpy(hst + gwB, tl.data(), tB);
     std::memcpy(hst + gwB + tB, tr.data(), tB);
     if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
-    SJBG_CK(h, cudaMemsetAsync(dTab, 0, slotB * slots, h->stream));
+    if (int rc_z = zero_fill(h, dTab, slotB * slots)) return rc_z;
     const GWin *dW = reinterpret_cast<const GWin *>(dev);
     const uint32_t *dTl = reinterpret_cast<const uint32_t *>(dev + gwB);
     const uint32_t *dTr = reinterpret_cast<const uint32_t *>(dev + gwB + tB);

@@ -103,6 +103,10 @@ int cuda_fail(sjbg_handle *h, cudaError_t e, const char *what);
 // Copy between pinned host staging and device memory with a kernel, in
 // stream order on the handle's stream (no copy engine involved).
 int stage_copy(sjbg_handle *h, void *dst, const void *src, size_t bytes);
+// Zero a ws_get buffer with SM stores (16-byte aligned, whole words): the
+// zeros stay in L2 for the kernels that use the buffer next, where a memset
+// may write them past L2.
+int zero_fill(sjbg_handle *h, void *dst, size_t bytes);
 
 // Device buffer of at least `bytes` in slot s (contents not preserved on growth).
 void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes);
