@@ -29,6 +29,7 @@
 // learned partitioner's prediction (learned.cu).
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "learned.cuh"
@@ -181,6 +182,16 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         __syncwarp();   // read before it is refilled
         wn = 0;
     };
+    // The counting loop, compiled once per kind of window (heavy keys, compacted
+    // light tuples, coarse output, learned or radix buckets), so that none of
+    // the mode tests runs per tuple.
+    auto count_tiles = [&](auto heavy_t, auto compact_t, auto coarse_t, auto learned_t) {
+    constexpr bool kHeavy = decltype(heavy_t)::value, kCompact = decltype(compact_t)::value;
+    constexpr bool kCoarse = decltype(coarse_t)::value, kLearned = decltype(learned_t)::value;
+    auto bucket_of = [&](uint32_t key) -> uint32_t {
+        if constexpr (kLearned) return learned_bucket(*cls.m, key);
+        else return key & cls.mask;
+    };
     // software pipeline: tile tt+1 is in flight while tile tt is counted
     uint2 nv[kPer];
     if (t_first < t_end) load_tile(t_first, nv);
@@ -199,7 +210,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         const bool valid = i < n;
         const uint32_t key = v[k].x, val = v[k].y;
         pk[k] = 0xFFFFFFFFu;
-        if (heavy) {
+        if constexpr (kHeavy) {
             const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
             if (hid != kHeavyBucket) {
                 const unsigned long long f = sjbg_fside(val, right ? 1u : 0u);   // one mix, either side
@@ -210,23 +221,24 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                 atomicAdd(&hsum_hi[a], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
             } else if (valid) {
                 // light keys: compacted windows count them in part_hist_light
-                if (compact) {
+                if constexpr (kCompact) {
                     lightmask |= 1u << k;
                 } else {
-                    const uint32_t b = cls.bucket(key);
+                    const uint32_t b = bucket_of(key);
                     atomicAdd(&hist[b], 1u);
-                    if (coarse) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
+                    if constexpr (kCoarse) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
                 }
             }
         } else {
             // plain partitioning: one shared atomic per tuple (measured faster
             // than combining a warp's equal buckets first, skewed keys included)
-            const uint32_t b = valid ? cls.bucket(key) : 0u;
+            const uint32_t b = valid ? bucket_of(key) : 0u;
             if (valid) atomicAdd(&hist[b], 1u);
-            if (coarse && valid) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
+            if constexpr (kCoarse)
+                if (valid) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
         }
     }
-    if (coarse) {
+    if constexpr (kCoarse) {
         SJBG_BARRIER();   // every rank of the tile is assigned
         uint32_t *row = rows_side + (uint64_t)(tp[w] + tt) * kRow;
         if (warp_id() == 0) {
@@ -265,7 +277,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         uint64_t *dst = coarse_out + (uint64_t)tt * kTile;
         for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) dst[i] = stage[i];
     }
-    if (compact) {
+    if constexpr (kCompact) {
         // the tile's light tuples go to the warp's buffer as (key,val) words
         // (warp scan, no block barrier); a full buffer is written out to the
         // window side's compact array with one global reservation
@@ -280,7 +292,18 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
         wn += wt;
     }
     }
-    if (compact && wn) flush_light();
+    if constexpr (kCompact)
+        if (wn) flush_light();
+    };
+    using T = std::true_type;
+    using F = std::false_type;
+    if (compact) count_tiles(T{}, T{}, F{}, T{});
+    else if (heavy && coarse) count_tiles(T{}, F{}, T{}, T{});
+    else if (heavy) count_tiles(T{}, F{}, F{}, T{});
+    else if (cls.m && coarse) count_tiles(F{}, F{}, T{}, T{});
+    else if (cls.m) count_tiles(F{}, F{}, F{}, T{});
+    else if (coarse) count_tiles(F{}, F{}, T{}, F{});
+    else count_tiles(F{}, F{}, F{}, F{});
     SJBG_BARRIER();
     uint32_t *dst = cnt + (right ? B : 0) + wp.bucket_base;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
