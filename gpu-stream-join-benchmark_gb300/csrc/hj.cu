@@ -186,114 +186,115 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     // light tuples, coarse output, learned or radix buckets), so that none of
     // the mode tests runs per tuple.
     auto count_tiles = [&](auto heavy_t, auto compact_t, auto coarse_t, auto learned_t) {
-    constexpr bool kHeavy = decltype(heavy_t)::value, kCompact = decltype(compact_t)::value;
-    constexpr bool kCoarse = decltype(coarse_t)::value, kLearned = decltype(learned_t)::value;
-    auto bucket_of = [&](uint32_t key) -> uint32_t {
-        if constexpr (kLearned) return learned_bucket(*cls.m, key);
-        else return key & cls.mask;
-    };
-    // software pipeline: tile tt+1 is in flight while tile tt is counted
-    uint2 nv[kPer];
-    if (t_first < t_end) load_tile(t_first, nv);
-    for (uint32_t tt = t_first; tt < t_end; tt++) {
-    const uint64_t start = (uint64_t)tt * kTile;
-    const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
-    uint2 v[kPer];
+        constexpr bool kHeavy = decltype(heavy_t)::value, kCompact = decltype(compact_t)::value;
+        constexpr bool kCoarse = decltype(coarse_t)::value, kLearned = decltype(learned_t)::value;
+        auto bucket_of = [&](uint32_t key) -> uint32_t {
+            if constexpr (kLearned) return learned_bucket(*cls.m, key);
+            else return key & cls.mask;
+        };
+        // software pipeline: tile tt+1 is in flight while tile tt is counted
+        uint2 nv[kPer];
+        if (t_first < t_end) load_tile(t_first, nv);
+        for (uint32_t tt = t_first; tt < t_end; tt++) {
+            const uint64_t start = (uint64_t)tt * kTile;
+            const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+            uint2 v[kPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) v[k] = nv[k];
-    if (tt + 1 < t_end) load_tile(tt + 1, nv);
-    uint32_t lightmask = 0;
-    uint32_t pk[kPer];   // coarse output: coarse << 16 | rank inside the tile's coarse run, or ~0u
+            for (int k = 0; k < kPer; k++) v[k] = nv[k];
+            if (tt + 1 < t_end) load_tile(tt + 1, nv);
+            uint32_t lightmask = 0;
+            uint32_t pk[kPer];   // coarse output: coarse << 16 | rank inside the tile's coarse run, or ~0u
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const uint32_t i = threadIdx.x + k * kPartThreads;
-        const bool valid = i < n;
-        const uint32_t key = v[k].x, val = v[k].y;
-        pk[k] = 0xFFFFFFFFu;
-        if constexpr (kHeavy) {
-            const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
-            if (hid != kHeavyBucket) {
-                const unsigned long long f = sjbg_fside(val, right ? 1u : 0u);   // one mix, either side
-                const uint32_t a = hid < kHotHeavy ? kMaxHeavy + 32u * hid + lane_id() : hid;
-                atomicAdd(&hcnt[a], 1u);
-                const uint32_t flo = (uint32_t)f;
-                const uint32_t old = atomicAdd(&hsum_lo[a], flo);
-                atomicAdd(&hsum_hi[a], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
-            } else if (valid) {
-                // light keys: compacted windows count them in part_hist_light
-                if constexpr (kCompact) {
-                    lightmask |= 1u << k;
+            for (int k = 0; k < kPer; k++) {
+                const uint32_t i = threadIdx.x + k * kPartThreads;
+                const bool valid = i < n;
+                const uint32_t key = v[k].x, val = v[k].y;
+                pk[k] = 0xFFFFFFFFu;
+                if constexpr (kHeavy) {
+                    const uint32_t hid = valid ? heavy_find(hs, key) : kHeavyBucket;
+                    if (hid != kHeavyBucket) {
+                        const unsigned long long f = sjbg_fside(val, right ? 1u : 0u);   // one mix, either side
+                        const uint32_t a = hid < kHotHeavy ? kMaxHeavy + 32u * hid + lane_id() : hid;
+                        atomicAdd(&hcnt[a], 1u);
+                        const uint32_t flo = (uint32_t)f;
+                        const uint32_t old = atomicAdd(&hsum_lo[a], flo);
+                        atomicAdd(&hsum_hi[a], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
+                    } else if (valid) {
+                        // light keys: compacted windows count them in part_hist_light
+                        if constexpr (kCompact) {
+                            lightmask |= 1u << k;
+                        } else {
+                            const uint32_t b = bucket_of(key);
+                            atomicAdd(&hist[b], 1u);
+                            if constexpr (kCoarse) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
+                        }
+                    }
                 } else {
-                    const uint32_t b = bucket_of(key);
-                    atomicAdd(&hist[b], 1u);
-                    if constexpr (kCoarse) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
+                    // plain partitioning: one shared atomic per tuple (measured faster
+                    // than combining a warp's equal buckets first, skewed keys included)
+                    const uint32_t b = valid ? bucket_of(key) : 0u;
+                    if (valid) atomicAdd(&hist[b], 1u);
+                    if constexpr (kCoarse)
+                        if (valid) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
                 }
             }
-        } else {
-            // plain partitioning: one shared atomic per tuple (measured faster
-            // than combining a warp's equal buckets first, skewed keys included)
-            const uint32_t b = valid ? bucket_of(key) : 0u;
-            if (valid) atomicAdd(&hist[b], 1u);
-            if constexpr (kCoarse)
-                if (valid) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
-        }
-    }
-    if constexpr (kCoarse) {
-        SJBG_BARRIER();   // every rank of the tile is assigned
-        uint32_t *row = rows_side + (uint64_t)(tp[w] + tt) * kRow;
-        if (warp_id() == 0) {
-            // exclusive offsets of the (at most 128) coarse runs; counters reset for the next tile
-            uint32_t a[kCoarseMax / 32], sum = 0;
+            if constexpr (kCoarse) {
+                SJBG_BARRIER();   // every rank of the tile is assigned
+                uint32_t *row = rows_side + (uint64_t)(tp[w] + tt) * kRow;
+                if (warp_id() == 0) {
+                    // exclusive offsets of the (at most 128) coarse runs; counters reset for the next tile
+                    uint32_t a[kCoarseMax / 32], sum = 0;
 #pragma unroll
-            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
-                const uint32_t c = lane_id() * (kCoarseMax / 32) + q;
-                a[q] = c < ncoarse ? ccnt_s[c] : 0u;
-                sum += a[q];
-            }
-            uint32_t tot;
-            uint32_t run = warp_excl_scan(sum, &tot);
+                    for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                        const uint32_t c = lane_id() * (kCoarseMax / 32) + q;
+                        a[q] = c < ncoarse ? ccnt_s[c] : 0u;
+                        sum += a[q];
+                    }
+                    uint32_t tot;
+                    uint32_t run = warp_excl_scan(sum, &tot);
 #pragma unroll
-            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
-                const uint32_t c = lane_id() * (kCoarseMax / 32) + q;
-                if (c < ncoarse) {
-                    cpre_s[c] = run;
-                    row[c] = run;
-                    ccnt_s[c] = 0;
+                    for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                        const uint32_t c = lane_id() * (kCoarseMax / 32) + q;
+                        if (c < ncoarse) {
+                            cpre_s[c] = run;
+                            row[c] = run;
+                            ccnt_s[c] = 0;
+                        }
+                        run += a[q];
+                    }
+                    if (lane_id() == 0) {
+                        cpre_s[ncoarse] = tot;
+                        row[ncoarse] = tot;
+                    }
                 }
-                run += a[q];
+                SJBG_BARRIER();
+#pragma unroll
+                for (int k = 0; k < kPer; k++)
+                    if (pk[k] != 0xFFFFFFFFu)
+                        stage[cpre_s[pk[k] >> 16] + (pk[k] & 0xFFFFu)] = ((uint64_t)v[k].y << 32) | v[k].x;
+                SJBG_BARRIER();
+                // the tile's light tuples, contiguous per coarse run, written out whole
+                const uint32_t nl = cpre_s[ncoarse];
+                uint64_t *dst = coarse_out + (uint64_t)tt * kTile;
+                for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) dst[i] = stage[i];
             }
-            if (lane_id() == 0) {
-                cpre_s[ncoarse] = tot;
-                row[ncoarse] = tot;
+            if constexpr (kCompact) {
+                // the tile's light tuples go to the warp's buffer as (key,val) words
+                // (warp scan, no block barrier); a full buffer is written out to the
+                // window side's compact array with one global reservation
+                const uint32_t nl = __popc(lightmask);
+                uint32_t wt;
+                const uint32_t ex = warp_excl_scan(nl, &wt);
+                if (wn + wt > kWarpBuf) flush_light();
+                uint32_t pos = wn + ex;
+#pragma unroll
+                for (int k = 0; k < kPer; k++)
+                    if ((lightmask >> k) & 1u) wbuf[pos++] = ((uint64_t)v[k].y << 32) | v[k].x;
+                wn += wt;
             }
         }
-        SJBG_BARRIER();
-#pragma unroll
-        for (int k = 0; k < kPer; k++)
-            if (pk[k] != 0xFFFFFFFFu) stage[cpre_s[pk[k] >> 16] + (pk[k] & 0xFFFFu)] = ((uint64_t)v[k].y << 32) | v[k].x;
-        SJBG_BARRIER();
-        // the tile's light tuples, contiguous per coarse run, written out whole
-        const uint32_t nl = cpre_s[ncoarse];
-        uint64_t *dst = coarse_out + (uint64_t)tt * kTile;
-        for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) dst[i] = stage[i];
-    }
-    if constexpr (kCompact) {
-        // the tile's light tuples go to the warp's buffer as (key,val) words
-        // (warp scan, no block barrier); a full buffer is written out to the
-        // window side's compact array with one global reservation
-        const uint32_t nl = __popc(lightmask);
-        uint32_t wt;
-        const uint32_t ex = warp_excl_scan(nl, &wt);
-        if (wn + wt > kWarpBuf) flush_light();
-        uint32_t pos = wn + ex;
-#pragma unroll
-        for (int k = 0; k < kPer; k++)
-            if ((lightmask >> k) & 1u) wbuf[pos++] = ((uint64_t)v[k].y << 32) | v[k].x;
-        wn += wt;
-    }
-    }
-    if constexpr (kCompact)
-        if (wn) flush_light();
+        if constexpr (kCompact)
+            if (wn) flush_light();
     };
     using T = std::true_type;
     using F = std::false_type;
