@@ -194,6 +194,29 @@ def test_learned_keeps_its_model_when_many_keys_are_hot(lib, oracle, z):
     assert (got["count"], got["prod"]) == (want["count"], want["prod"]) == (rad["count"], rad["prod"])
 
 
+@pytest.mark.parametrize("z", [1.5, 1.0, 0.5])
+def test_config_skewed_8x2p24_full_size(lib, oracle, z):
+    """The skewed workload at its full size: 8 windows of 2^24 tuples per stream,
+    keys Zipf(z) over [0, 2^24) with ranks permuted (seed 3), R seed 1, S seed 2.
+    In every window, learned partitioning and radix partitioning at 2^10 both
+    equal the oracle's count and prod."""
+    D, W, nw = 1 << 24, 1 << 24, 8
+    table = oracle.zipf_table(D, z)
+    left = oracle.gen_zipf(0, nw * W, 1, table, D, 3, threads=16)
+    right = oracle.gen_zipf(0, nw * W, 2, table, D, 3, threads=16)
+    descs = [(w * W, W, w * W, W, 0, 0) for w in range(nw)]
+    want, _ = oracle.join_windows(left, right, descs, enumerate_pairs=False, threads=16)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=W) as j:
+        got = j.lazy_execute_batch(left, right, descs)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, radix_bits=10,
+                    max_tuples_per_window=W) as j:
+        rad = j.lazy_execute_batch(left, right, descs)
+    for i, (g, r, w) in enumerate(zip(got, rad, want)):
+        assert (g["count"], g["prod"]) == (w["count"], w["prod"]) == (r["count"], r["prod"]), i
+    if z == 1.5:
+        assert all(g["partitioner_used"] == lib.PART_LEARNED for g in got)
+
+
 def test_learned_keeps_radix_when_it_is_cheaper(lib, oracle):
     """Zipf z = 0.5 over 2^24 keys: heavy keys hold well under a tenth of the
     sample and radix buckets it evenly, so the learned partitioner keeps radix
