@@ -60,7 +60,7 @@ struct LearnedModel : LearnedCore {
 static_assert(sizeof(LearnedCore) % 16 == 0, "LearnedCore is copied in 16-byte units");
 static_assert(sizeof(HeavySet) % 16 == 0, "HeavySet is copied in 16-byte units");
 static_assert(sizeof(LearnedModel) % 16 == 0, "models are stored back to back");
-static_assert(offsetof(LearnedModel, heavy_set) % 16 == 0, "the heavy set is copied in 16-byte units");
+static_assert(alignof(HeavySet) == 16, "the heavy set (a member at a 16-byte multiple) is copied in 16-byte units");
 
 // Per-window, per-heavy-key aggregates.
 struct HeavyAcc {
