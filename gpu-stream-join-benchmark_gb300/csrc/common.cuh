@@ -83,6 +83,13 @@ __device__ __forceinline__ void flush_acc(WinAcc *acc, unsigned long long count,
     }
 }
 
+// hi + the carry out of a + b (two instructions: add with carry-out, add with carry-in).
+__device__ __forceinline__ uint32_t add_carry(uint32_t hi, uint32_t a, uint32_t b) {
+    uint32_t r;
+    asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %1, %2;\n\taddc.u32 %0, %3, 0;\n\t}" : "=r"(r) : "r"(a), "r"(b), "r"(hi));
+    return r;
+}
+
 // Exclusive warp prefix sum of a 32-bit value.
 __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t *total) {
     uint32_t x = v;

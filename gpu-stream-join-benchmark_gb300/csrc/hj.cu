@@ -204,10 +204,13 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
             if (tt + 1 < t_end) load_tile(tt + 1, nv);
             uint32_t lightmask = 0;
             uint32_t pk[kPer];   // coarse output: coarse << 16 | rank inside the tile's coarse run, or ~0u
+            // the tuples of a tile, compiled apart for full tiles (no bounds test)
+            auto count_tuples = [&](auto full_t) {
+            constexpr bool kFull = decltype(full_t)::value;
 #pragma unroll
             for (int k = 0; k < kPer; k++) {
                 const uint32_t i = threadIdx.x + k * kPartThreads;
-                const bool valid = i < n;
+                const bool valid = kFull || i < n;
                 const uint32_t key = v[k].x, val = v[k].y;
                 pk[k] = 0xFFFFFFFFu;
                 if constexpr (kHeavy) {
@@ -218,7 +221,7 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                         atomicAdd(&hcnt[a], 1u);
                         const uint32_t flo = (uint32_t)f;
                         const uint32_t old = atomicAdd(&hsum_lo[a], flo);
-                        atomicAdd(&hsum_hi[a], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
+                        atomicAdd(&hsum_hi[a], add_carry((uint32_t)(f >> 32), old, flo));
                     } else if (valid) {
                         // light keys: compacted windows count them in part_hist_light
                         if constexpr (kCompact) {
@@ -238,6 +241,9 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
                         if (valid) pk[k] = ((b >> cshift) << 16) | atomicAdd(&ccnt_s[b >> cshift], 1u);
                 }
             }
+            };
+            if (n == (uint32_t)kTile) count_tuples(std::true_type{});
+            else count_tuples(std::false_type{});
             if constexpr (kCoarse) {
                 SJBG_BARRIER();   // every rank of the tile is assigned
                 uint32_t *row = rows_side + (uint64_t)(tp[w] + tt) * kRow;
@@ -882,7 +888,7 @@ __device__ __forceinline__ void ct_add_sum(unsigned long long *slot, unsigned lo
     uint32_t *w2 = reinterpret_cast<uint32_t *>(slot);   // little-endian: low word first
     const uint32_t flo = (uint32_t)f;
     const uint32_t old = atomicAdd(&w2[0], flo);
-    atomicAdd(&w2[1], (uint32_t)(f >> 32) + (old + flo < old ? 1u : 0u));
+    atomicAdd(&w2[1], add_carry((uint32_t)(f >> 32), old, flo));
 }
 
 // Insert `c` tuples of `key` with fr-sum `f`.  A key that finds neither itself
