@@ -235,13 +235,13 @@ def test_learned_keeps_radix_when_it_is_cheaper(lib, oracle):
 
 def test_learned_heavy_keys_sharing_a_set_bucket(lib, oracle):
     """The heavy-key set has 2,048 buckets of two slots (bucket = top 11 bits of
-    key * 0x9E3779B97F4A7C15).  Four heavy keys of one bucket: the two heaviest
+    key * 0x9E3779B1 mod 2^32).  Four heavy keys of one bucket: the two heaviest
     take its slots, the other two find it full and stay light, and are joined
     through the partitions; the result still equals the oracle and radix."""
-    C, M = 0x9E3779B97F4A7C15, (1 << 64) - 1
+    C, M = 0x9E3779B1, (1 << 32) - 1
     by_bucket = {}
     for k in range(1, 1 << 20):
-        group = by_bucket.setdefault(((k * C) & M) >> 53, [])
+        group = by_bucket.setdefault(((k * C) & M) >> 21, [])
         group.append(k)
         if len(group) == 4:
             break
