@@ -38,7 +38,7 @@
 namespace sjbg {
 
 constexpr int kTile = 4096;          // tuples per partitioning tile
-constexpr uint32_t kHistTiles = 16;  // tiles per histogram CTA (amortises its set-up)
+constexpr uint32_t kHistTiles = 16;  // tiles per counting CTA at least (amortises its set-up)
 constexpr int kPartThreads = 512;
 constexpr int kJoinThreads = 512;
 constexpr uint32_t kMaxBucketsLog2 = 14;
@@ -115,7 +115,8 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     // that hold the same hot key update it without bank conflicts.
     constexpr uint32_t kHeavySlotsAcc = kMaxHeavy + 32 * kHotHeavy;
     __shared__ uint32_t hcnt[kHeavySlotsAcc], hsum_lo[kHeavySlotsAcc], hsum_hi[kHeavySlotsAcc];
-    // this CTA covers tiles [t, t + kHistTiles) of one window side ("hist groups")
+    // this CTA covers an equal share of one window side's tiles: the side has
+    // hgroup[w + 1] - hgroup[w] counting CTAs ("hist groups")
     const bool right = blockIdx.x >= hgroupL[nwin];
     const uint32_t g = right ? blockIdx.x - hgroupL[nwin] : blockIdx.x;
     const uint32_t *hp = right ? hgroupR : hgroupL;
@@ -141,8 +142,9 @@ part_hist_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict_
     if (coarse)
         for (uint32_t i = threadIdx.x; i < ncoarse; i += blockDim.x) ccnt_s[i] = 0;
     const uint64_t nside = right ? wp.n_right : wp.n_left;
-    const uint32_t t_first = (g - hp[w]) * kHistTiles;            // tile index inside the window
-    const uint32_t t_end = min(t_first + kHistTiles, tp[w + 1] - tp[w]);
+    const uint32_t side_tiles = tp[w + 1] - tp[w], ncta = hp[w + 1] - hp[w], j = g - hp[w];
+    const uint32_t t_first = (uint32_t)((uint64_t)j * side_tiles / ncta);   // tile indices inside the window side
+    const uint32_t t_end = (uint32_t)((uint64_t)(j + 1) * side_tiles / ncta);
     // counters of the buckets in use: the model's own fan-out when there is one
     const uint32_t P = 1u << (cls.m ? cls.m->log2_buckets : wp.log2_buckets);
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
@@ -1238,8 +1240,6 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         maxP = std::max(maxP, 1u << lg);
         tileL[w + 1] = tileL[w] + (uint32_t)((wh.n_left + kTile - 1) / kTile);
         tileR[w + 1] = tileR[w] + (uint32_t)((wh.n_right + kTile - 1) / kTile);
-        hgL[w + 1] = hgL[w] + (tileL[w + 1] - tileL[w] + kHistTiles - 1) / kHistTiles;
-        hgR[w + 1] = hgR[w] + (tileR[w + 1] - tileR[w] + kHistTiles - 1) / kHistTiles;
         // fine-pass CTAs: coarse partitions x groups of kGroupTiles tiles
         const uint32_t nc = 1u << coarse_bits(lg);
         itL[w + 1] = itL[w] + nc * ((tileL[w + 1] - tileL[w] + kGroupTiles - 1) / kGroupTiles);
@@ -1251,6 +1251,30 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     }
     if (B > 0xFFFFFFFFull / 4 || totL >= 0xFFFFFFFFull || totR >= 0xFFFFFFFFull)
         return fail(h, SJBG_E_CAPACITY, "hash join batch exceeds 2^32 tuples per side");
+    // counting CTAs per window side: shares of about T / (resident CTAs) tiles
+    // (at least kHistTiles), so that one wave holds the call when its window
+    // sides are large and the set-up of each CTA is paid over many tiles.
+    // When many sides are smaller than a share (uneven batches), shares of an
+    // eighth of that keep the CTAs small enough to balance the SMs.
+    {
+        const size_t histSmem = sizeof(uint32_t) * ((maxP + 1) / 2 * 2) + sizeof(uint64_t) * kTile;
+        allow_big_smem(part_hist_kernel, histSmem);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_hist_kernel, kPartThreads, histSmem) !=
+            cudaSuccess)
+            return fail(h, SJBG_E_CUDA, "counting pass occupancy");
+        const uint64_t slots = (uint64_t)std::max(per_sm, 1) * (uint64_t)std::max(h->num_sms, 1);
+        const uint64_t T = (uint64_t)tileL[n] + tileR[n];
+        uint64_t share = std::max<uint64_t>(kHistTiles, (T + slots - 1) / slots);
+        uint64_t ctas = 0;
+        for (uint32_t w = 0; w < n; w++)
+            ctas += (tileL[w + 1] - tileL[w] + share - 1) / share + (tileR[w + 1] - tileR[w] + share - 1) / share;
+        if (ctas > slots + slots / 8) share = std::max<uint64_t>(kHistTiles, T / (8 * slots));
+        for (uint32_t w = 0; w < n; w++) {
+            hgL[w + 1] = hgL[w] + (uint32_t)((tileL[w + 1] - tileL[w] + share - 1) / share);
+            hgR[w + 1] = hgR[w] + (uint32_t)((tileR[w + 1] - tileR[w] + share - 1) / share);
+        }
+    }
     std::vector<uint32_t> bwin(B);
     for (uint32_t w = 0; w < n; w++)
         for (uint32_t k = 0; k < (1u << plan[w].log2_buckets); k++) bwin[plan[w].bucket_base + k] = w;
@@ -1319,7 +1343,6 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     const uint32_t tiles = tileL[n] + tileR[n];
     if (tiles) {
         const size_t histSmem = sizeof(uint32_t) * ((maxP + 1) / 2 * 2) + sizeof(uint64_t) * kTile;
-        allow_big_smem(part_hist_kernel, histSmem);
         SJBG_CK(h, launch(h, "part_hist", part_hist_kernel, dim3(hgL[n] + hgR[n]), dim3(kPartThreads), histSmem, dL,
                           dR, dPlan, n, dTileL, dTileR, dHgL, dHgR, dCnt, (uint32_t)B, dModels, dHeavy, dComp, dCompR,
                           dCcnt, dRows));
