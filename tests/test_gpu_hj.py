@@ -217,6 +217,22 @@ def test_config_skewed_8x2p24_full_size(lib, oracle, z):
         assert all(g["partitioner_used"] == lib.PART_LEARNED for g in got)
 
 
+def test_learned_keeps_its_model_on_streaming_keys(lib, oracle):
+    """The streaming workload's keys: Zipf z = 1.2 over 2^26 with ranks permuted
+    (seed 3).  The heavy set must place the heaviest keys, so that none is left
+    in a light partition it would overflow, and the model does not fall back to
+    radix partitioning; the result equals the oracle."""
+    D, W = 1 << 26, 1 << 23
+    table = oracle.zipf_table(D, 1.2)
+    left = oracle.gen_zipf(0, W, 1, table, D, 3, threads=16)
+    right = oracle.gen_zipf(0, W, 2, table, D, 3, threads=16)
+    want = oracle.join(left, right, enumerate_pairs=False)
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=W) as j:
+        got = j.lazy_execute(left, right)
+    assert got["partitioner_used"] == lib.PART_LEARNED and not (got["flags"] & lib.WR_FALLBACK)
+    assert (got["count"], got["prod"]) == (want["count"], want["prod"])
+
+
 def test_learned_keeps_radix_when_it_is_cheaper(lib, oracle):
     """Zipf z = 0.5 over 2^24 keys: heavy keys hold well under a tenth of the
     sample and radix buckets it evenly, so the learned partitioner keeps radix
@@ -235,13 +251,13 @@ def test_learned_keeps_radix_when_it_is_cheaper(lib, oracle):
 
 def test_learned_heavy_keys_sharing_a_set_bucket(lib, oracle):
     """The heavy-key set has 2,048 buckets of two slots (bucket = top 11 bits of
-    key * 0x9E3779B1 mod 2^32).  Four heavy keys of one bucket: the two heaviest
+    key * 0x9E3779B97F4A7C15).  Four heavy keys of one bucket: the two heaviest
     take its slots, the other two find it full and stay light, and are joined
     through the partitions; the result still equals the oracle and radix."""
-    C, M = 0x9E3779B1, (1 << 32) - 1
+    C, M = 0x9E3779B97F4A7C15, (1 << 64) - 1
     by_bucket = {}
     for k in range(1, 1 << 20):
-        group = by_bucket.setdefault(((k * C) & M) >> 21, [])
+        group = by_bucket.setdefault(((k * C) & M) >> 53, [])
         group.append(k)
         if len(group) == 4:
             break
