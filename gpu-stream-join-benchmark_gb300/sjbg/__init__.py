@@ -69,6 +69,18 @@ class WindowResult(C.Structure):
                 "partitioner_used": self.partitioner_used, "ms": self.ms}
 
 
+def window_dicts(res) -> list:
+    """The windows of a WindowResult array filled by sjbg_eager_run: entries
+    past the stream's last window carry status E_INVALID and are dropped.  Only
+    the windows themselves are converted (a per-entry loop over all 2n + 2
+    slots costs milliseconds of host time per call)."""
+    mw = len(res)
+    words = np.frombuffer(res, dtype=np.uint32).reshape(mw, C.sizeof(WindowResult) // 4)
+    absent = np.flatnonzero(words[:, WindowResult.status.offset // 4] == 1)
+    n = int(absent[0]) if absent.size else mw
+    return [res[i].as_dict() for i in range(n)]
+
+
 class WindowDesc(C.Structure):
     _fields_ = [("left_offset", C.c_uint64), ("n_left", C.c_uint64), ("right_offset", C.c_uint64),
                 ("n_right", C.c_uint64), ("pairs_offset", C.c_uint64), ("pairs_capacity", C.c_uint64)]
@@ -262,13 +274,7 @@ class Joiner:
         res = (WindowResult * mw)()
         self._check(self.lib.sjbg_eager_run(self.h, _ptr(left), _ptr(right), n_batches, mem, _ptr(bc),
                                             C.cast(res, C.c_void_p), mw))
-        # entries past the stream's last window carry status E_INVALID; only the
-        # windows themselves are converted (a per-entry loop over all 2n + 2 slots
-        # costs milliseconds of host time per call)
-        words = np.frombuffer(res, dtype=np.uint32).reshape(mw, C.sizeof(WindowResult) // 4)
-        absent = np.flatnonzero(words[:, WindowResult.status.offset // 4] == 1)
-        n = int(absent[0]) if absent.size else mw
-        return bc, [res[i].as_dict() for i in range(n)]
+        return bc, window_dicts(res)
 
     # ---- streaming
     def stream_open(self, window_ns: int):

@@ -75,3 +75,26 @@ def test_null_handle_calls_return_invalid(lib):
     assert L.sjbg_kernel_stats_reset(None) == 1
     assert L.sjbg_launch_count(None) == 0
     assert L.sjbg_version() == 1
+
+
+def test_eager_run_results_stop_at_the_first_absent_window():
+    """sjbg_eager_run fills one result per window and status E_INVALID after the
+    last one; the binding returns exactly the windows (no kernel runs here)."""
+    import sjbg
+
+    res = (sjbg.WindowResult * 8)()
+    for i in range(8):
+        res[i].count = 100 + i
+        res[i].prod_checksum = 7 * i
+        res[i].flags = sjbg.WR_XOR if i == 1 else 0
+        res[i].xor_checksum = 99
+        res[i].status = 0 if i < 3 else 1
+    wins = sjbg.window_dicts(res)
+    assert [w["count"] for w in wins] == [100, 101, 102]
+    assert [w["prod"] for w in wins] == [0, 7, 14]
+    assert [w["xor"] for w in wins] == [None, 99, None]
+    for i in range(8):
+        res[i].status = 0
+    assert len(sjbg.window_dicts(res)) == 8
+    res[0].status = 1
+    assert sjbg.window_dicts(res) == []
