@@ -54,6 +54,20 @@ int cuda_fail(sjbg_handle *h, cudaError_t e, const char *what) {
     return fail(h, e == cudaErrorMemoryAllocation ? SJBG_E_NOMEM : SJBG_E_CUDA, m);
 }
 
+cudaError_t raise_smem_limit(const void *kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> granted;   // (device, kernel) -> limit set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    size_t &cur = granted[{dev, kernel}];
+    if (bytes <= cur) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
 void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes) {
     DevBuf &b = h->ws[s];
     bytes = std::max<size_t>(16, (bytes + 15) & ~(size_t)15);   // whole 16-byte words (stage_copy, zero_fill)

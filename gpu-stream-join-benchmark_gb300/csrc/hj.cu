@@ -1424,8 +1424,35 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
 struct RawScratch {
     WinPlan plan;
     uint32_t tile[8];   // tileL {0, tL}, tileR {0, tR}, hgL {0, gL}, hgR {0, gR}
-    WinAcc acc;
+    WinAcc acc[2];      // the window's accumulator, then the call's device status word (acc[1].info, kErr* bits)
 };
+
+// Byte offsets of the scratch buffers from a 256-byte aligned base: the
+// RawScratch record, the bucket arrays (bucket_win P words, counts, starts and
+// cursors 2P words each) and the partitioned sides (8 bytes per tuple).  The
+// size check of the entry point and the carving below both use it.
+struct RawLayout {
+    size_t rs, bwin, part_left, part_right, end;
+};
+
+static size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+static RawLayout raw_layout(uint64_t nL, uint64_t nR, uint32_t P) {
+    RawLayout l;
+    l.rs = 0;
+    l.bwin = round256(sizeof(RawScratch));
+    l.part_left = l.bwin + round256(sizeof(uint32_t) * 7 * (size_t)P);
+    l.part_right = l.part_left + sizeof(uint64_t) * std::max<uint64_t>(nL, 1);
+    l.end = l.part_right + sizeof(uint64_t) * std::max<uint64_t>(nR, 1);
+    return l;
+}
+
+// Radix fan-out of a window: about 4,096 left tuples per bucket; one bucket when a side is empty.
+static uint32_t raw_log2_buckets(uint64_t nL, uint64_t nR) {
+    uint32_t lg = 0;
+    while (((uint64_t)4096 << lg) < nL) lg++;
+    return (nL == 0 || nR == 0) ? 0 : lg;
+}
 
 __global__ void raw_setup_kernel(RawScratch *rs, uint32_t *bucket_win, uint32_t *cnt, uint32_t P, uint64_t nL,
                                  uint64_t nR, uint32_t lg, uint32_t tL, uint32_t tR) {
@@ -1438,7 +1465,8 @@ __global__ void raw_setup_kernel(RawScratch *rs, uint32_t *bucket_win, uint32_t 
         rs->tile[2] = 0; rs->tile[3] = tR;
         rs->tile[4] = 0; rs->tile[5] = (tL + kHistTiles - 1) / kHistTiles;
         rs->tile[6] = 0; rs->tile[7] = (tR + kHistTiles - 1) / kHistTiles;
-        rs->acc = WinAcc{0, 0, 0, 0, 0};
+        rs->acc[0] = WinAcc{0, 0, 0, 0, 0};
+        rs->acc[1] = WinAcc{0, 0, 0, 0, 0};
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * P; i += gridDim.x * blockDim.x) {
         cnt[i] = 0;
@@ -1446,14 +1474,19 @@ __global__ void raw_setup_kernel(RawScratch *rs, uint32_t *bucket_win, uint32_t 
     }
 }
 
+// The window's result, with the device status word turned into a status code
+// (the bits the batched path maps in device_status_error).
 __global__ void raw_finish_kernel(const RawScratch *rs, sjbg_window_result *out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const unsigned long long bits = rs->acc[1].info;
         sjbg_window_result r;
-        r.count = rs->acc.count;
+        r.count = rs->acc[0].count;
         r.xor_checksum = 0;
-        r.prod_checksum = rs->acc.prod;
+        r.prod_checksum = rs->acc[0].prod;
         r.n_pairs = 0;
-        r.status = SJBG_OK;
+        r.status = !bits ? SJBG_OK
+                         : (bits & kErrTimeout) ? SJBG_E_TIMEOUT
+                                                : SJBG_E_CAPACITY;   // a table or queue could not take its input
         r.flags = 0;
         r.partitioner_used = SJBG_PART_RADIX;
         r.ms = 0.0f;
@@ -1462,53 +1495,62 @@ __global__ void raw_finish_kernel(const RawScratch *rs, sjbg_window_result *out)
 }
 
 size_t hj_raw_scratch_bytes(uint64_t max_tuples) {
-    const uint64_t P = (max_tuples + 4095) / 4096;
-    return 256 * 4 + sizeof(RawScratch) + 256 + 4 * 4 * P + 256 + 2 * 8 * max_tuples + 1024;
+    const uint32_t P = 1u << raw_log2_buckets(max_tuples, max_tuples);
+    return 255 + raw_layout(max_tuples, max_tuples, P).end;   // 255: aligning the caller's base
 }
 
 static uint8_t *align256(uint8_t *p) { return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255)); }
 
 int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR, uint64_t nR, uint8_t *sc,
                         size_t sc_bytes, sjbg_window_result *dOut, cudaStream_t st) {
-    uint32_t lg = 0;
-    while (((uint64_t)4096 << lg) < nL) lg++;
-    if (nL == 0 || nR == 0) lg = 0;
+    const uint32_t lg = raw_log2_buckets(nL, nR);
     const uint32_t P = 1u << lg;
     const uint32_t tL = (uint32_t)((nL + kTile - 1) / kTile), tR = (uint32_t)((nR + kTile - 1) / kTile);
-    uint8_t *p = align256(sc);
-    RawScratch *rs = reinterpret_cast<RawScratch *>(p);
-    p = align256(p + sizeof(RawScratch));
-    uint32_t *bwin = reinterpret_cast<uint32_t *>(p);
+    uint8_t *base = align256(sc);
+    const RawLayout lay = raw_layout(nL, nR, P);
+    if (base + lay.end > sc + sc_bytes)
+        return fail(nullptr, SJBG_E_CAPACITY, "sjbg_lazy_hj_noalloc: the window does not fit the fixed scratch");
+    RawScratch *rs = reinterpret_cast<RawScratch *>(base + lay.rs);
+    uint32_t *bwin = reinterpret_cast<uint32_t *>(base + lay.bwin);
     uint32_t *cnt = bwin + P;
     uint32_t *start = cnt + 2 * P;
     uint32_t *cur = start + 2 * P;
-    p = align256(reinterpret_cast<uint8_t *>(cur + 2 * P));
-    uint64_t *pL = reinterpret_cast<uint64_t *>(p);
-    uint64_t *pR = pL + std::max<uint64_t>(nL, 1);
-    if (reinterpret_cast<uint8_t *>(pR + std::max<uint64_t>(nR, 1)) > sc + sc_bytes) return SJBG_E_CAPACITY;
+    uint64_t *pL = reinterpret_cast<uint64_t *>(base + lay.part_left);
+    uint64_t *pR = reinterpret_cast<uint64_t *>(base + lay.part_right);
+    // an error left pending by the caller's own earlier work is not this call's
+    cudaGetLastError();
+    auto launched = [](const char *what) -> int {
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? SJBG_OK : cuda_fail(nullptr, e, what);
+    };
     raw_setup_kernel<<<4, 256, 0, st>>>(rs, bwin, cnt, P, nL, nR, lg, tL, tR);
+    if (int rc = launched("sjbg_lazy_hj_noalloc: raw_setup_kernel")) return rc;
     const uint32_t *tl = rs->tile;
-    if (tL + tR) {
+    if (tL && tR) {
         const uint32_t groups = (tL + kHistTiles - 1) / kHistTiles + (tR + kHistTiles - 1) / kHistTiles;
         allow_big_smem(part_hist_kernel, sizeof(uint32_t) * P);
         part_hist_kernel<<<groups, kPartThreads, sizeof(uint32_t) * P, st>>>(
             dL, dR, &rs->plan, 1, tl, tl + 2, tl + 4, tl + 6, cnt, P, nullptr, nullptr, nullptr, nullptr, nullptr,
             nullptr);
+        if (int rc = launched("sjbg_lazy_hj_noalloc: part_hist_kernel")) return rc;
         part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);
+        if (int rc = launched("sjbg_lazy_hj_noalloc: part_scan_kernel")) return rc;
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * P;
         allow_big_smem(part_scatter_kernel, scatterSmem);
         // a single-level radix window: the scatter work is every tile
         part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, tl, tl + 2,
                                                                           cur, P, pL, pR, nullptr, nullptr, nullptr,
                                                                           nullptr);
+        if (int rc = launched("sjbg_lazy_hj_noalloc: part_scatter_kernel")) return rc;
         const uint32_t cap = count_table_cap(4096);
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
-        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, &rs->acc, cap, nullptr,
+        bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, rs->acc, cap, nullptr,
                                                                 nullptr, nullptr);
+        if (int rc = launched("sjbg_lazy_hj_noalloc: bucket_join_count_kernel")) return rc;
     }
     raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);
-    return cudaGetLastError() == cudaSuccess ? SJBG_OK : SJBG_E_CUDA;
+    return launched("sjbg_lazy_hj_noalloc: raw_finish_kernel");
 }
 
 }  // namespace sjbg

@@ -140,9 +140,15 @@ cudaError_t launch(sjbg_handle *h, const char *name, void (*kernel)(KArgs...), d
     return e;
 }
 
+// Raise a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`.  The limit is process-wide state of the kernel, shared by
+// every handle and thread, so it is only ever raised: a call asking for less
+// than a concurrent caller's launch needs leaves that launch's limit alone.
+cudaError_t raise_smem_limit(const void *kernel, size_t bytes);
+
 template <typename K>
 void allow_big_smem(K kernel, size_t bytes) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    raise_smem_limit(reinterpret_cast<const void *>(kernel), bytes);
 }
 
 // ---- host-side window description used by the join modules -------------

@@ -125,8 +125,12 @@ static void harvest(sjbg_handle *h, StreamState &st, bool wait) {
             r.status = SJBG_E_BUDGET;
             st.rejected++;
         }
-        r.n_pairs = w->id;   // streaming results carry the window id in n_pairs
-        st.ready.push_back(r);
+        sjbg_stream_window sw;
+        sw.result = r;
+        sw.window_id = w->id;
+        sw.n_left = w->n[0];
+        sw.n_right = w->n[1];
+        st.ready.push_back(sw);
         release_buffers(h, st, w);
         st.wins.pop_front();
         st.spare.push_back(w);
@@ -312,7 +316,7 @@ int sjbg_stream_push(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int is
     return SJBG_OK;
 }
 
-int sjbg_stream_poll(sjbg_handle *h, sjbg_window_result *out, uint32_t max_out, uint32_t *n_out) {
+int sjbg_stream_poll(sjbg_handle *h, sjbg_stream_window *out, uint32_t max_out, uint32_t *n_out) {
     if (!h || !n_out || (max_out && !out)) return SJBG_E_INVALID;
     StreamState *st = ss(h);
     if (!st) return fail(h, SJBG_E_STATE, "stream not open");

@@ -28,7 +28,7 @@ struct StreamState {
     uint64_t used = 0;           // bytes held by window buffers
     std::deque<StreamWin *> wins;      // open and in-flight windows, by id
     std::vector<StreamWin *> spare;    // recycled window records
-    std::deque<sjbg_window_result> ready;
+    std::deque<sjbg_stream_window> ready;
     std::vector<double> lat_ms;
     uint64_t closed = 0, rejected = 0, joined = 0, fallbacks = 0, last_closed_id = 0;
     bool any_closed = false;

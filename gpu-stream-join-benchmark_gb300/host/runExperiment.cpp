@@ -9,7 +9,8 @@
 //
 // Optional keys with no reference counterpart: dataSize (tuples per stream,
 // default 2560 MiB of tuples), sourceThreads (default 32), tsUpperBound
-// (default 1000).  --list prints the expanded configurations and their
+// (default 1000), gpuDevice (CUDA device of the joiners and of the power
+// sampler, default 0).  --list prints the expanded configurations and their
 // algorithm names without touching a GPU.
 #include <cuda_runtime.h>
 
@@ -123,7 +124,7 @@ std::pair<std::string, uint64_t> runExperimentWithConfig(const ExperimentConfig 
         Sink sink;
         auto windowing = Windowing::WindowingFactory::create(config.algorithmConfig, config.dataConfig,
                                                              config.queryConfig, config.engineConfig, sink);
-        PowerSampler power;   // power_data.txt, as the reference writes it
+        PowerSampler power("power_data.txt", 10, config.engineConfig.gpuDevice);   // as the reference writes it
         if (config.measurePower) power.start();
         auto t0 = std::chrono::high_resolution_clock::now();
         sink.markProcessingStart();
@@ -297,6 +298,7 @@ int main(int argc, char **argv) {
         if (y.has("dataSize")) ec.dataConfig.dataSize = std::stoull(y.scalar("dataSize"));
         if (y.has("sourceThreads")) ec.sourceThreads = std::stoull(y.scalar("sourceThreads"));
         if (y.has("tsUpperBound")) ec.dataConfig.timestampUpperBound = std::stoull(y.scalar("tsUpperBound"));
+        if (y.has("gpuDevice")) ec.engineConfig.gpuDevice = std::stoi(y.scalar("gpuDevice"));
         const std::string metric = y.scalar("measuredMetric");
         if (metric != "Throughput" && metric != "cumulativePercentage")
             throw std::invalid_argument("Unknown measured metrics: " + metric);

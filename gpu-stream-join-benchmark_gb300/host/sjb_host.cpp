@@ -2,6 +2,8 @@
 // GPU joiners of libsjbg.  See sjb_host.hpp for the reference file of each class.
 #include "sjb_host.hpp"
 
+#include <cuda_runtime.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cctype>
@@ -163,12 +165,23 @@ CountBased::CountBased(Sink &sink, uint64_t ringBufferSize, uint64_t ringBufferM
         available[0].push_back(i * batchSize);
         available[1].push_back(i * batchSize);
     }
-    // Left uninitialised: pages are committed as batches are written.
-    ring[0].reset(new Tuple[ringBufferSize]);
-    ring[1].reset(new Tuple[ringBufferSize]);
+    // Pinned, as the reference's ring (include/sjb/windowing/lazy/CountBased.cuh:35-36), so the
+    // joiners' host-to-device copies of a window's batches run at the link's rate.
+    for (int s = 0; s < 2; s++) {
+        void *p = nullptr;
+        if (cudaMallocHost(&p, sizeof(Tuple) * ringBufferSize) != cudaSuccess) {
+            cudaGetLastError();
+            if (ring[0]) cudaFreeHost(ring[0]);
+            throw std::runtime_error("CountBased: cudaMallocHost of the ring buffer failed");
+        }
+        ring[s] = static_cast<Tuple *>(p);
+    }
 }
 
-CountBased::~CountBased() = default;
+CountBased::~CountBased() {
+    for (Tuple *r : ring)
+        if (r) cudaFreeHost(r);
+}
 
 void CountBased::incoming(Tuple *batch, int side) {
     uint64_t slot = 0;
@@ -185,7 +198,7 @@ void CountBased::incoming(Tuple *batch, int side) {
         if (trial > ringBufferMaxTries) throw std::runtime_error("Ring buffer is full");
         std::this_thread::sleep_for(std::chrono::microseconds(1));
     }
-    std::copy(batch, batch + batchSize, ring[side].get() + slot);
+    std::copy(batch, batch + batchSize, ring[side] + slot);
     {
         std::lock_guard<std::mutex> g(mu);
         executable[side].push_back(slot);
@@ -211,7 +224,7 @@ void CountBased::execute() {
     auto joiner = impl->pool.pop();
     ExecutionStatistic st;
     try {
-        st = joiner->execute(ring[0].get(), ring[1].get(), li, ri, sink);
+        st = joiner->execute(ring[0], ring[1], li, ri, sink);
     } catch (...) {
         impl->pool.push(joiner);
         throw;
@@ -236,7 +249,6 @@ void CountBased::execute() {
 namespace Eager {
 
 void CountBased::closeWindowIfFull(bool &closed) {
-    std::lock_guard<std::mutex> g(mu);
     if (total[0] >= windowSize || total[1] >= windowSize) {
         harvestChecksums();
         joiner->clearStates();
@@ -254,6 +266,7 @@ void CountBased::harvestChecksums() {
 }
 
 void CountBased::incoming(Tuple *batch, bool left) {
+    std::lock_guard<std::mutex> g(mu);
     bool closed = false;
     closeWindowIfFull(closed);
     const int me = left ? 0 : 1;
@@ -328,7 +341,7 @@ sjbg_config WindowingFactory::toConfig(const AlgorithmConfig &a, const DataConfi
     c.max_tuples_per_window = std::max<uint64_t>(e.maxTupleInWindow, q.windowSize);
     c.window_size = q.windowSize;
     c.num_distinct_keys = d.numDistinctKey;
-    c.device = 0;
+    c.device = e.gpuDevice;
     return c;
 }
 
@@ -388,6 +401,7 @@ struct Nvml {
     int (*init)() = nullptr;
     int (*shutdown)() = nullptr;
     int (*handle)(unsigned, void **) = nullptr;
+    int (*handle_pci)(const char *, void **) = nullptr;
     int (*power)(void *, unsigned *) = nullptr;   // milliwatts
     bool load() {
         lib = dlopen("libnvidia-ml.so.1", RTLD_NOW | RTLD_LOCAL);
@@ -395,6 +409,7 @@ struct Nvml {
         init = reinterpret_cast<int (*)()>(dlsym(lib, "nvmlInit_v2"));
         shutdown = reinterpret_cast<int (*)()>(dlsym(lib, "nvmlShutdown"));
         handle = reinterpret_cast<int (*)(unsigned, void **)>(dlsym(lib, "nvmlDeviceGetHandleByIndex_v2"));
+        handle_pci = reinterpret_cast<int (*)(const char *, void **)>(dlsym(lib, "nvmlDeviceGetHandleByPciBusId_v2"));
         power = reinterpret_cast<int (*)(void *, unsigned *)>(dlsym(lib, "nvmlDeviceGetPowerUsage"));
         return init && shutdown && handle && power;
     }
@@ -405,7 +420,11 @@ bool PowerSampler::start() {
     if (thread) return true;
     auto *nv = new Nvml();
     void *dev = nullptr;
-    if (!nv->load() || nv->init() != 0 || nv->handle(0, &dev) != 0) {
+    char bus[32] = {0};
+    const bool have_bus = cudaDeviceGetPCIBusId(bus, (int)sizeof(bus), device) == cudaSuccess;
+    if (!have_bus) cudaGetLastError();
+    if (!nv->load() || nv->init() != 0 ||
+        (have_bus && nv->handle_pci ? nv->handle_pci(bus, &dev) : nv->handle((unsigned)device, &dev)) != 0) {
         std::fprintf(stderr, "runExperiment: NVML unavailable, power is not measured\n");
         if (nv->lib) dlclose(nv->lib);
         delete nv;

@@ -127,6 +127,7 @@ struct EngineConfig {
     uint64_t joinerThreads;
     uint64_t nSourceThreads;
     uint64_t maxTupleInWindow;
+    int gpuDevice = 0;   // CUDA device of the GPU joiners (no reference counterpart)
 };
 
 namespace Windowing {
@@ -218,7 +219,7 @@ private:
     struct Impl;
     uint64_t ringBufferSize, ringBufferMaxTries, windowSize, batchSize;
     std::unique_ptr<Impl> impl;
-    std::unique_ptr<Tuple[]> ring[2];
+    Tuple *ring[2] = {nullptr, nullptr};   // pinned host memory (cudaMallocHost), as the reference's
     std::deque<uint64_t> available[2], executable[2];
     std::mutex mu;
 };
@@ -238,9 +239,15 @@ public:
 
 private:
     void incoming(Tuple *batch, bool left);
-    void closeWindowIfFull(bool &closed);
-    void harvestChecksums();
+    void closeWindowIfFull(bool &closed);   // caller holds mu
+    void harvestChecksums();                // caller holds mu
     uint64_t windowSize, batchSize;
+    // Tuples of the current window per side.  The close check, the batch's
+    // execution and the update of total[] happen under mu as one step, so
+    // source threads that deliver batches concurrently cannot both close a
+    // window or count a batch into a window that was just closed (the
+    // reference reads and writes these counters without a lock,
+    // include/sjb/windowing/eager/CountBased.cuh:47-49).
     uint64_t total[2] = {0, 0};
     std::shared_ptr<Executor::BaseEagerExecutor> joiner;
     std::mutex mu;
@@ -275,14 +282,15 @@ private:
 // GPU power sampling while an experiment runs (measurePowerUsage: "Yes"),
 // the role of the reference's PowerMeasurementAgent
 // (src/sjb/utils/PowerMeasurementAgent.cpp:50-175): a thread reads the board
-// power of GPU 0 through NVML every `period_ms` and appends "epoch_ms,watts"
-// lines to a file.  NVML is loaded at run time; when it is missing, start()
-// says so on stderr and the experiment runs unmeasured.  Read-only: no GPU
-// setting is changed.
+// power of the CUDA device `device` (the one the joiners run on; NVML finds it
+// by its PCI bus id, so CUDA_VISIBLE_DEVICES renumbering does not matter)
+// through NVML every `period_ms` and appends "epoch_ms,watts" lines to a file.
+// NVML is loaded at run time; when it is missing, start() says so on stderr
+// and the experiment runs unmeasured.  Read-only: no GPU setting is changed.
 class PowerSampler {
 public:
-    explicit PowerSampler(std::string path = "power_data.txt", unsigned period_ms = 10)
-        : path(std::move(path)), period_ms(period_ms) {}
+    explicit PowerSampler(std::string path = "power_data.txt", unsigned period_ms = 10, int device = 0)
+        : path(std::move(path)), period_ms(period_ms), device(device) {}
     ~PowerSampler() { end(); }
     bool start();
     void end();
@@ -291,6 +299,7 @@ public:
 private:
     std::string path;
     unsigned period_ms;
+    int device;
     std::atomic<bool> run{false};
     std::atomic<unsigned> n{0};
     void *thread = nullptr;   // std::thread, kept opaque

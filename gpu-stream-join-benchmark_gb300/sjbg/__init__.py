@@ -86,6 +86,16 @@ class WindowDesc(C.Structure):
                 ("n_right", C.c_uint64), ("pairs_offset", C.c_uint64), ("pairs_capacity", C.c_uint64)]
 
 
+class StreamWindow(C.Structure):
+    _fields_ = [("result", WindowResult), ("window_id", C.c_uint64), ("n_left", C.c_uint64),
+                ("n_right", C.c_uint64)]
+
+    def as_dict(self):
+        d = self.result.as_dict()
+        d.update(window_id=self.window_id, n_left=self.n_left, n_right=self.n_right)
+        return d
+
+
 class StreamStats(C.Structure):
     _fields_ = [("windows_closed", C.c_uint64), ("tuples_joined", C.c_uint64), ("windows_rejected", C.c_uint64),
                 ("fallbacks", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("busy_ms", C.c_double)]
@@ -285,7 +295,8 @@ class Joiner:
                                               int(is_left), mem))
 
     def stream_poll(self, max_out=1024):
-        res = (WindowResult * max_out)()
+        """Closed windows in id order: result fields plus window_id, n_left, n_right."""
+        res = (StreamWindow * max_out)()
         n = C.c_uint32()
         self._check(self.lib.sjbg_stream_poll(self.h, C.cast(res, C.c_void_p), max_out, C.byref(n)))
         return [res[i].as_dict() for i in range(n.value)]

@@ -257,11 +257,21 @@ typedef struct sjbg_stream_stats {
     double busy_ms;
 } sjbg_stream_stats;
 
+/* One closed event-time window: its result (n_pairs is 0: the loop writes
+ * no pairs), the window's id (tuples with floor(ts / window_ns) == window_id)
+ * and how many tuples each side contributed. */
+typedef struct sjbg_stream_window {
+    sjbg_window_result result;
+    uint64_t window_id;
+    uint64_t n_left;
+    uint64_t n_right;
+} sjbg_stream_window;
+
 SJBG_API int sjbg_stream_open(sjbg_handle *h, uint64_t window_ns);
 /* Push one batch (ts = event time in ns, non-decreasing per side). */
 SJBG_API int sjbg_stream_push(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int is_left, uint32_t mem);
-/* Retrieve closed windows' results; *n_out receives how many were written. */
-SJBG_API int sjbg_stream_poll(sjbg_handle *h, sjbg_window_result *out, uint32_t max_out, uint32_t *n_out);
+/* Retrieve closed windows' results in window-id order; *n_out receives how many were written. */
+SJBG_API int sjbg_stream_poll(sjbg_handle *h, sjbg_stream_window *out, uint32_t max_out, uint32_t *n_out);
 SJBG_API int sjbg_stream_close(sjbg_handle *h, sjbg_stream_stats *stats);
 
 /* ---- synthetic inputs on the device ---------------------------------------------
@@ -284,7 +294,9 @@ SJBG_API int sjbg_zipf_table(uint64_t *table, uint64_t n, double z);
  * copies nothing from the host.  left/right (n_left, n_right <= 2^20 tuples,
  * else SJBG_E_CAPACITY) and out are DEVICE memory; the work is enqueued on
  * cuda_stream (NULL = the legacy default stream) and out is written when it
- * completes.  Needs no handle.  Its scratch is a fixed 17 MiB device array
+ * completes, with out->status carrying what the kernels reported on the
+ * device (SJBG_OK, or SJBG_E_TIMEOUT / SJBG_E_CAPACITY).  The return value
+ * covers the argument checks and the launches.  Needs no handle.  Its scratch is a fixed 17 MiB device array
  * that every GPU loading the library holds until exit; the first call on a
  * device looks up that array's address and should come before any stream
  * capture.  Calls share the array: calls that overlap on the GPU race and

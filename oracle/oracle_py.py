@@ -9,7 +9,8 @@ Two libraries:
     sorted pairs).  Built from source on first use.
   * ``_ref/libsjbref.so`` - the reference's own CPU joiner sources compiled
     against the TBB-API shim (``make -C oracle ref``).  Only available where
-    the reference sources are mounted; ``ref_lib()`` returns None elsewhere.
+    the reference sources are present (``SJB_REF_SRC``); ``ref_lib()``
+    returns None elsewhere.
 """
 from __future__ import annotations
 
@@ -23,7 +24,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUPLE_DTYPE = np.dtype([("key", "<u4"), ("val", "<u4"), ("ts", "<u8")])
 PAIR_DTYPE = np.dtype([("r", "<u4"), ("s", "<u4")])
-REF_SRC = "/root/reference"
 
 _lock = threading.Lock()
 _lib = None
@@ -50,10 +50,11 @@ def build(force: bool = False) -> str:
 
 
 def build_ref() -> str | None:
-    """Compile the reference's CPU joiners when their sources are present."""
+    """Compile the reference's CPU joiners when their sources are present
+    (the recipe's `ref-if-present` target; the location comes from the
+    SJB_REF_SRC environment variable or the recipe's default)."""
     so = os.path.join(HERE, "_ref", "libsjbref.so")
-    if os.path.isdir(os.path.join(REF_SRC, "src")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"], check=True, stdout=subprocess.DEVNULL)
     return so if os.path.exists(so) else None
 
 

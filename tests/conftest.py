@@ -10,7 +10,6 @@ for p in (PKG, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REF_SRC = "/root/reference"
 
 
 def pytest_configure(config):

@@ -42,9 +42,10 @@ def test_struct_layouts_match_header(lib):
 #include <stddef.h>
 #include "sjbg.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(sjbg_tuple), sizeof(sjbg_pair), sizeof(sjbg_config),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sjbg_tuple), sizeof(sjbg_pair), sizeof(sjbg_config),
          sizeof(sjbg_window_result), sizeof(sjbg_window_desc), sizeof(sjbg_stream_stats),
-         offsetof(sjbg_config, hbm_budget_bytes));
+         offsetof(sjbg_config, hbm_budget_bytes), sizeof(sjbg_stream_window),
+         offsetof(sjbg_stream_window, window_id));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as d:
@@ -54,7 +55,8 @@ int main(void) {
         subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert sizes == [16, 8, C.sizeof(lib.Config), C.sizeof(lib.WindowResult), C.sizeof(lib.WindowDesc),
-                     C.sizeof(lib.StreamStats), lib.Config.hbm_budget_bytes.offset]
+                     C.sizeof(lib.StreamStats), lib.Config.hbm_budget_bytes.offset, C.sizeof(lib.StreamWindow),
+                     lib.StreamWindow.window_id.offset]
     assert lib.TUPLE_DTYPE.itemsize == 16 and lib.PAIR_DTYPE.itemsize == 8
 
 

@@ -49,7 +49,7 @@ def test_stream_windows_match_oracle(lib, oracle):
             results += j.stream_poll()
         stats = j.stream_close()
         results += j.stream_poll()
-    by_id = {r["n_pairs"]: r for r in results}   # the window id travels in n_pairs
+    by_id = {r["window_id"]: r for r in results}
     wl, wr = left["ts"] // W_NS, right["ts"] // W_NS
     ids = sorted(set(wl.tolist()) | set(wr.tolist()))
     assert stats["windows_closed"] == len(ids) and stats["windows_rejected"] == 0

@@ -1,14 +1,12 @@
 """CPU tests of the oracle: pinned against the golden fixtures made by the
 reference's own CPU joiners, known-answer windows, and (where the reference
-sources are mounted) a live cross-check of restatement vs reference."""
-import os
-
+sources are present, see SJB_REF_SRC in oracle/Makefile) a live cross-check of
+restatement vs reference."""
 import numpy as np
 import pytest
 
 from helpers import load_fixture, make_tuples, sorted_pairs
 
-REF_PRESENT = os.path.isdir("/root/reference/src")
 
 
 # ------------------------------------------------------------------ generator pins
@@ -160,9 +158,9 @@ def test_lazy_hj_precondition(oracle):
 
 
 # ------------------------------------------------------------------ live cross-check with the reference
-@pytest.mark.skipif(not REF_PRESENT, reason="reference sources not mounted")
 def test_restatement_equals_reference_live(oracle):
-    assert oracle.ref_lib() is not None
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference's CPU joiners are not built here (no reference sources)")
     rng = np.random.default_rng(3)
     for dk, n, B in ((64, 1024, 128), (1000, 4096, 512), (1 << 12, 8192, 1024)):
         l = make_tuples(rng.integers(0, dk, n))
