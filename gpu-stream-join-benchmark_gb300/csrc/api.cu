@@ -581,6 +581,7 @@ int sjbg_create(const sjbg_config *cfg, sjbg_handle **out) {
 
 int sjbg_destroy(sjbg_handle *h) {
     if (!h) return SJBG_E_INVALID;
+    eager_shutdown(h);
     if (h->stream) cudaStreamSynchronize(h->stream);
     delete h;
     return SJBG_OK;

@@ -28,60 +28,18 @@
 #include <cstring>
 #include <vector>
 
-#include "eager.cuh"
+#include "eager_dev.cuh"
 
 namespace sjbg {
 
 int nlj_pair_launch(sjbg_handle *h, const sjbg_tuple *L, uint64_t nL, const sjbg_tuple *R, uint64_t nR, WinAcc *acc,
                     unsigned long long *batch_count, sjbg_pair *pairs, uint64_t pairs_cap, bool enumerate);
 
-EagerState::~EagerState() {
-    for (void *p : allocs) cudaFree(p);
-}
-
-constexpr uint32_t kNilIdx = 0xFFFFFFFFu;
 constexpr uint32_t kPrefixTile = 4096;
 
-struct ETab {
-    uint32_t *keys, *cnt, *head, *next;
-    unsigned long long *sum;
-    uint32_t bits;
-};
-
-__device__ __forceinline__ int etab_lookup(const ETab &t, uint32_t key) {
-    const uint32_t C = 1u << t.bits;
-    if (key == kEmptyKey) return t.cnt[C] ? (int)C : -1;
-    uint32_t s = slot_hash(key, t.bits);
-    for (uint32_t p = 0; p < C; p++) {
-        const uint32_t k = t.keys[s];
-        if (k == key) return (int)s;
-        if (k == kEmptyKey) return -1;
-        s = (s + 1) & (C - 1);
-    }
-    return -1;
-}
-
-__device__ __forceinline__ uint32_t etab_claim(const ETab &t, uint32_t key) {
-    const uint32_t C = 1u << t.bits;
-    if (key == kEmptyKey) return C;
-    uint32_t s = slot_hash(key, t.bits);
-    for (uint32_t p = 0; p < C; p++) {   // the table is at most half full
-        const uint32_t prev = atomicCAS(&t.keys[s], kEmptyKey, key);
-        if (prev == kEmptyKey || prev == key) return s;
-        s = (s + 1) & (C - 1);
-    }
-    return C;   // unreachable by sizing
-}
-
-__device__ __forceinline__ unsigned long long own_hash(int side, uint32_t val) {
-    return sjbg_fside(val, side == 0 ? 0u : 1u);
-}
-
-__device__ __forceinline__ void flush_batch(WinAcc *acc, unsigned long long *bcount, unsigned long long count,
-                                            unsigned long long xr, unsigned long long prod) {
-    flush_acc(acc, count, xr, prod);
-    const unsigned long long c = warp_sum_u64(count);
-    if (lane_id() == 0 && c) atomicAdd(bcount, c);
+EagerState::~EagerState() {
+    pk.reset();   // the persistent kernel (if any) has returned before its buffers go
+    for (void *p : allocs) cudaFree(p);
 }
 
 // ---------------------------------------------------------------- hash join
@@ -98,45 +56,8 @@ eager_hj_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32_t base,
         key = t.x;
         val = t.y;
     }
-    const unsigned long long oh = own_hash(side, val);
-    unsigned long long count = 0, xr = 0, prod = 0;
-    uint32_t head = kNilIdx, mine = 0;
-    if (valid) {
-        const int s = etab_lookup(oth, key);
-        if (s >= 0) {
-            mine = oth.cnt[s];
-            count = mine;
-            prod = oh * oth.sum[s];
-            head = oth.head[s];
-        }
-    }
-    // chains hold indices of the other side's tuples; walks stop at its size
-    if (kEnum) {
-        uint32_t steps = 0;
-        for (uint32_t j = head; j < oth_n && steps < oth_n; j = oth.next[j], steps++) {
-            const uint32_t ov = oth_tuples[j].val;
-            xr ^= side == 0 ? sjbg_pair_hash(val, ov) : sjbg_pair_hash(ov, val);
-        }
-    }
-    if (kPairs) {
-        uint32_t tot;
-        const uint32_t ex = warp_excl_scan(mine, &tot);
-        unsigned long long b = 0;
-        if (lane_id() == 0 && tot) b = atomicAdd(&acc->npairs, (unsigned long long)tot);
-        b = __shfl_sync(0xFFFFFFFFu, b, 0) + ex;
-        uint32_t steps = 0;
-        for (uint32_t j = head; j < oth_n && steps < oth_n; j = oth.next[j], b++, steps++) {
-            const uint32_t ov = oth_tuples[j].val;
-            if (b < pcap) pairs[b] = side == 0 ? sjbg_pair{val, ov} : sjbg_pair{ov, val};
-        }
-    }
-    if (valid) {   // add the tuple to its own side's table
-        const uint32_t s = etab_claim(own, key);
-        atomicAdd(&own.cnt[s], 1u);
-        atomicAdd(&own.sum[s], oh);
-        own.next[base + i] = atomicExch(&own.head[s], base + i);
-    }
-    flush_batch(acc, bcount, count, xr, prod);
+    eager_hj_step<kEnum, kPairs>(valid, key, val, base + i, side, own, oth, oth_tuples, oth_n, acc, bcount, pairs,
+                                 pcap);
 }
 
 // ---------------------------------------------------------------- sort-merge join
@@ -173,23 +94,6 @@ eager_sort_batch_kernel(const sjbg_tuple *__restrict__ batch, uint32_t n, uint32
         out_keys[i] = (uint32_t)(sv[i] >> 32);
         out_vals[i] = (uint32_t)sv[i];
     }
-}
-
-__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *a, uint32_t n, uint32_t key) {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (a[mid] < key) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-__device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t *a, uint32_t n, uint32_t key) {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (a[mid] <= key) lo = mid + 1; else hi = mid;
-    }
-    return lo;
 }
 
 template <bool kEnum, bool kPairs>
@@ -510,6 +414,14 @@ static int eager_check(sjbg_handle *h) {
     return SJBG_OK;
 }
 
+static bool persistent(const sjbg_handle *h) { return (h->cfg.flags & SJBG_F_PERSISTENT) != 0; }
+
+int eager_shutdown(sjbg_handle *h) {
+    if (!h->eager || !h->eager->pk) return SJBG_OK;
+    cudaSetDevice(h->device);
+    return pk_stop(h, false);
+}
+
 }  // namespace sjbg
 
 using namespace sjbg;
@@ -521,6 +433,7 @@ int sjbg_eager_execute(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int 
     int rc = eager_check(h);
     if (rc) return rc;
     if ((n && !batch) || (mem != SJBG_MEM_HOST && mem != SJBG_MEM_DEVICE)) return fail(h, SJBG_E_INVALID, "bad batch");
+    if (persistent(h)) return pk_execute(h, batch, n, is_left ? 0 : 1, mem == SJBG_MEM_HOST, match_count);
     EagerState &st = *h->eager;
     SJBG_CK(h, cudaMemsetAsync(st.batch_count, 0, 8, h->stream));
     rc = eager_enqueue(h, batch, n, is_left ? 0 : 1, mem == SJBG_MEM_HOST, st.batch_count);
@@ -537,6 +450,7 @@ int sjbg_eager_execute(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int 
 int sjbg_eager_clear_states(sjbg_handle *h) {
     int rc = eager_check(h);
     if (rc) return rc;
+    if (persistent(h)) return pk_clear_states(h);
     rc = eager_clear(h);
     if (rc) return rc;
     SJBG_CK(h, cudaStreamSynchronize(h->stream));
@@ -547,15 +461,24 @@ int sjbg_eager_window_result(sjbg_handle *h, sjbg_pair *pairs, uint64_t pairs_ca
     int rc = eager_check(h);
     if (rc) return rc;
     if (!out) return fail(h, SJBG_E_INVALID, "null result");
-    WinAcc *ha = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc)));
-    if (!ha) return fail(h, SJBG_E_NOMEM, "result staging");
-    SJBG_CK(h, cudaMemcpyAsync(ha, h->eager->acc, sizeof(WinAcc), cudaMemcpyDeviceToHost, h->stream));
-    SJBG_CK(h, cudaStreamSynchronize(h->stream));
-    fill_eager_result(h, *ha, out);
+    if (persistent(h)) {   // the totals after every ticket posted so far
+        WinAcc totals;
+        if ((rc = pk_report(h, &totals))) return rc;
+        fill_eager_result(h, totals, out);
+    } else {
+        WinAcc *ha = static_cast<WinAcc *>(pinned_get(h, 3, sizeof(WinAcc)));
+        if (!ha) return fail(h, SJBG_E_NOMEM, "result staging");
+        SJBG_CK(h, cudaMemcpyAsync(ha, h->eager->acc, sizeof(WinAcc), cudaMemcpyDeviceToHost, h->stream));
+        SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        fill_eager_result(h, *ha, out);
+    }
     if (pairs && h->eager->pairs) {
         const uint64_t np = std::min(out->n_pairs, pairs_capacity);
-        if (np)
-            SJBG_CK(h, cudaMemcpy(pairs, h->eager->pairs, sizeof(sjbg_pair) * np, cudaMemcpyDeviceToHost));
+        if (np) {   // (on the handle's stream: a running persistent kernel does not block the copy)
+            SJBG_CK(h, cudaMemcpyAsync(pairs, h->eager->pairs, sizeof(sjbg_pair) * np, cudaMemcpyDeviceToHost,
+                                       h->stream));
+            SJBG_CK(h, cudaStreamSynchronize(h->stream));
+        }
         if (np < out->n_pairs) out->flags |= SJBG_WR_PAIRS_TRUNCATED;
         out->n_pairs = np;
     } else {
@@ -567,8 +490,32 @@ int sjbg_eager_window_result(sjbg_handle *h, sjbg_pair *pairs, uint64_t pairs_ca
 int sjbg_eager_end_of_stream(sjbg_handle *h) {
     int rc = eager_check(h);
     if (rc) return rc;
+    if (persistent(h) && (rc = pk_stop(h, false))) return rc;
     SJBG_CK(h, cudaStreamSynchronize(h->stream));
     return SJBG_OK;
+}
+
+int sjbg_eager_post(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int is_left, uint32_t mem,
+                    uint64_t *ticket) {
+    int rc = eager_check(h);
+    if (rc) return rc;
+    if (!persistent(h)) return fail(h, SJBG_E_STATE, "sjbg_eager_post needs an SJBG_F_PERSISTENT handle");
+    if ((n && !batch) || (mem != SJBG_MEM_HOST && mem != SJBG_MEM_DEVICE)) return fail(h, SJBG_E_INVALID, "bad batch");
+    return pk_post_batch(h, batch, n, is_left ? 0 : 1, mem == SJBG_MEM_HOST, ticket);
+}
+
+int sjbg_eager_wait(sjbg_handle *h, uint64_t ticket, uint64_t *match_count) {
+    int rc = eager_check(h);
+    if (rc) return rc;
+    if (!persistent(h)) return fail(h, SJBG_E_STATE, "sjbg_eager_wait needs an SJBG_F_PERSISTENT handle");
+    return pk_wait_batch(h, ticket, match_count);
+}
+
+int sjbg_eager_pk_status(sjbg_handle *h, int *running, uint64_t *launches) {
+    int rc = eager_check(h);
+    if (rc) return rc;
+    if (!persistent(h)) return fail(h, SJBG_E_STATE, "not an SJBG_F_PERSISTENT handle");
+    return pk_status(h, running, launches);
 }
 
 int sjbg_eager_run(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *right, uint64_t n_batches, uint32_t mem,
@@ -576,6 +523,8 @@ int sjbg_eager_run(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *rig
     int rc = eager_check(h);
     if (rc) return rc;
     if (n_batches && (!left || !right)) return fail(h, SJBG_E_INVALID, "null stream");
+    // the whole-stream path replaces the window state a persistent kernel keeps
+    if (persistent(h) && (rc = pk_stop(h, true))) return rc;
     const uint64_t B = h->cfg.batch_size;
     // host streams are copied to the device once
     const sjbg_tuple *dl = left, *dr = right;

@@ -22,6 +22,11 @@ struct EagerSide {
     unsigned long long *F = nullptr;   // n + 1 entries
 };
 
+struct PkState;   // persistent eager kernel (eager_pk.cu)
+struct PkDeleter {
+    void operator()(PkState *p) const;
+};
+
 struct EagerState {
     EagerSide side[2];
     uint64_t cap = 0;          // tuples per side
@@ -32,6 +37,7 @@ struct EagerState {
     uint64_t pairs_cap = 0;
     uint32_t *sort_tmp = nullptr;  // sorted incoming batch: keys then vals (2 * kEagerMaxSortBatch)
     std::vector<void *> allocs;
+    std::unique_ptr<PkState, PkDeleter> pk;   // SJBG_F_PERSISTENT: created by the first ticket
     ~EagerState();
 };
 
@@ -56,5 +62,17 @@ int eager_run_batched(sjbg_handle *h, const sjbg_tuple *dl, const sjbg_tuple *dr
 
 int eager_init(sjbg_handle *h);
 int eager_init_and_clear(sjbg_handle *h);
+
+// Persistent eager kernel (eager_pk.cu), used by the eager entry points of
+// SJBG_F_PERSISTENT handles.
+int pk_execute(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int side, bool from_host, uint64_t *match);
+int pk_post_batch(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int side, bool from_host, uint64_t *ticket);
+int pk_wait_batch(sjbg_handle *h, uint64_t ticket, uint64_t *match);
+int pk_clear_states(sjbg_handle *h);
+int pk_report(sjbg_handle *h, WinAcc *totals);
+int pk_stop(sjbg_handle *h, bool reset);
+int pk_status(sjbg_handle *h, int *running, uint64_t *launches);
+// Stop a handle's persistent kernel before the handle goes.
+int eager_shutdown(sjbg_handle *h);
 
 }  // namespace sjbg

@@ -28,7 +28,7 @@ EAGER, LAZY = 0, 1
 RESULT_NO_OUTPUT, RESULT_COUNT_KERNEL, RESULT_ESTIMATED_SELECTIVITY, RESULT_BITMAP, RESULT_ATOMIC = 0, 1, 2, 3, 4
 PART_AUTO, PART_NONE, PART_RADIX, PART_LEARNED = 0, 1, 2, 3
 MEM_HOST, MEM_DEVICE = 0, 1
-F_XOR, F_PROFILE, F_AUTOTUNE, F_VERIFY, F_GRAPH = 0x1, 0x2, 0x4, 0x8, 0x10
+F_XOR, F_PROFILE, F_AUTOTUNE, F_VERIFY, F_GRAPH, F_PERSISTENT = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 WR_XOR, WR_PAIRS_TRUNCATED, WR_FALLBACK, WR_RADIX_BY_COST = 0x1, 0x2, 0x4, 0x8
 
 STATUS = {0: "OK", 1: "E_INVALID", 2: "E_NOMEM", 3: "E_CUDA", 4: "E_TIMEOUT", 5: "E_CAPACITY",
@@ -38,6 +38,7 @@ EXPORTS = [
     "sjbg_create", "sjbg_destroy", "sjbg_last_error", "sjbg_set_stream", "sjbg_version",
     "sjbg_lazy_execute", "sjbg_lazy_execute_ring", "sjbg_lazy_execute_batch",
     "sjbg_eager_execute", "sjbg_eager_clear_states", "sjbg_eager_window_result", "sjbg_eager_end_of_stream",
+    "sjbg_eager_post", "sjbg_eager_wait", "sjbg_eager_pk_status",
     "sjbg_eager_run", "sjbg_stream_open", "sjbg_stream_push", "sjbg_stream_poll", "sjbg_stream_close",
     "sjbg_generate", "sjbg_kernel_stats", "sjbg_kernel_stats_reset", "sjbg_launch_count",
     "sjbg_lazy_hj_noalloc", "sjbg_zipf_table",
@@ -55,7 +56,8 @@ class Config(C.Structure):
                 ("partitioner", C.c_uint32), ("batch_size", C.c_uint64), ("max_tuples_per_window", C.c_uint64),
                 ("window_size", C.c_uint64), ("num_distinct_keys", C.c_uint64), ("flags", C.c_uint32),
                 ("radix_bits", C.c_uint32), ("learned_leaves", C.c_uint32), ("sample_rate", C.c_float),
-                ("overflow_bound", C.c_float), ("device", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+                ("overflow_bound", C.c_float), ("device", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
+                ("idle_timeout_ms", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class WindowResult(C.Structure):
@@ -127,6 +129,9 @@ def load(path: str = LIB_PATH):
         L.sjbg_eager_clear_states.argtypes = [vp]
         L.sjbg_eager_window_result.argtypes = [vp, vp, u64, C.POINTER(WindowResult)]
         L.sjbg_eager_end_of_stream.argtypes = [vp]
+        L.sjbg_eager_post.argtypes = [vp, vp, u64, i32, u32, C.POINTER(u64)]
+        L.sjbg_eager_wait.argtypes = [vp, u64, C.POINTER(u64)]
+        L.sjbg_eager_pk_status.argtypes = [vp, C.POINTER(i32), C.POINTER(u64)]
         L.sjbg_eager_run.argtypes = [vp, vp, vp, u64, u32, vp, vp, u32]
         L.sjbg_stream_open.argtypes = [vp, u64]
         L.sjbg_stream_push.argtypes = [vp, vp, u64, i32, u32]
@@ -188,11 +193,11 @@ class Joiner:
     def __init__(self, algorithm=ALG_HJ, progressiveness=LAZY, result_mode=RESULT_NO_OUTPUT,
                  partitioner=PART_AUTO, batch_size=0, max_tuples_per_window=1 << 26, window_size=0,
                  num_distinct_keys=0, flags=0, radix_bits=0, learned_leaves=0, sample_rate=0.0,
-                 overflow_bound=0.0, device=0, hbm_budget_bytes=0):
+                 overflow_bound=0.0, device=0, hbm_budget_bytes=0, idle_timeout_ms=0):
         self.lib = load()
         self.cfg = Config(algorithm, progressiveness, result_mode, partitioner, batch_size, max_tuples_per_window,
                           window_size, num_distinct_keys, flags, radix_bits, learned_leaves, sample_rate,
-                          overflow_bound, device, hbm_budget_bytes)
+                          overflow_bound, device, hbm_budget_bytes, idle_timeout_ms, 0)
         h = C.c_void_p()
         rc = self.lib.sjbg_create(C.byref(self.cfg), C.byref(h))
         if rc:
@@ -277,6 +282,28 @@ class Joiner:
 
     def eager_end_of_stream(self):
         self._check(self.lib.sjbg_eager_end_of_stream(self.h))
+
+    def eager_post(self, batch, is_left: bool, mem=MEM_HOST, n=None) -> int:
+        """Post a batch to the persistent kernel (F_PERSISTENT handles); returns its ticket."""
+        t = C.c_uint64()
+        self._check(self.lib.sjbg_eager_post(self.h, _ptr(batch), n if n is not None else _len(batch),
+                                             int(is_left), mem, C.byref(t)))
+        return t.value
+
+    def eager_wait(self, ticket: int) -> int:
+        """New matches of a posted batch."""
+        c = C.c_uint64()
+        self._check(self.lib.sjbg_eager_wait(self.h, ticket, C.byref(c)))
+        return c.value
+
+    def eager_pk_status(self):
+        """(status code, running, launches) of the persistent kernel; status 4
+        (E_TIMEOUT) once after the kernel's wait for the next batch ran out."""
+        running, launches = C.c_int32(), C.c_uint64()
+        rc = self.lib.sjbg_eager_pk_status(self.h, C.byref(running), C.byref(launches))
+        if rc not in (0, 4):
+            self._check(rc)
+        return rc, bool(running.value), launches.value
 
     def eager_run(self, left, right, n_batches, mem=MEM_HOST, max_windows=None):
         bc = np.zeros(2 * n_batches, np.uint64)

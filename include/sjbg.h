@@ -116,6 +116,7 @@ enum { SJBG_MEM_HOST = 0, SJBG_MEM_DEVICE = 1 };
 #define SJBG_F_AUTOTUNE 0x4u  /* pick buckets / tiles / fan-out by measurement */
 #define SJBG_F_VERIFY   0x8u  /* learned partitioning: also run radix and compare */
 #define SJBG_F_GRAPH    0x10u /* capture batched lazy calls on device inputs in a CUDA graph, replay repeats */
+#define SJBG_F_PERSISTENT 0x20u /* eager: one resident kernel takes batches from a queue (the reference's usePK) */
 
 /* sjbg_window_result.flags */
 #define SJBG_WR_XOR             0x1u /* xor_checksum is valid */
@@ -142,6 +143,8 @@ typedef struct sjbg_config {
     float overflow_bound;           /* learned: worst partition / mean partition allowed, 0 = 8 */
     int32_t device;                 /* CUDA device ordinal */
     uint64_t hbm_budget_bytes;      /* streaming admission budget, 0 = no limit */
+    uint32_t idle_timeout_ms;       /* SJBG_F_PERSISTENT: longest wait of the kernel for the next batch, 0 = 1000 */
+    uint32_t reserved;              /* 0 */
 } sjbg_config;
 
 typedef struct sjbg_window_result {
@@ -244,6 +247,39 @@ SJBG_API int sjbg_eager_end_of_stream(sjbg_handle *h);
 SJBG_API int sjbg_eager_run(sjbg_handle *h, const sjbg_tuple *left, const sjbg_tuple *right,
                    uint64_t n_batches, uint32_t mem,
                    uint64_t *batch_counts, sjbg_window_result *out, uint32_t n_windows_out);
+
+/* ---- persistent eager joins (SJBG_F_PERSISTENT) ----------------------------------
+ * Replaces the reference's persistent-kernel executor GPU_HJ_PK
+ * (src/sjb/windowing/eager/executor/GPU/GPU_HJ_PK.cu:10-89,101-180; chosen by
+ * EagerJoinConfig::usePK, include/experiment/Config.hpp:15).  On an eager
+ * handle created with SJBG_F_PERSISTENT, one cooperative kernel stays resident
+ * on the device and takes tickets (batches, and the clear / report / stop
+ * commands behind sjbg_eager_clear_states, sjbg_eager_window_result and
+ * sjbg_eager_end_of_stream) from a queue in mapped host memory, in order.
+ * sjbg_eager_execute then posts its batch and reads the count from a mapped
+ * result slot: no launch, copy-engine transfer or stream synchronisation per
+ * batch.  Pinned host batches are read by the kernel in place; pageable ones
+ * are copied into the queue.  Hash join (HJ) takes up to 32 SMs; nested-loop
+ * and sort-merge joins take the whole GPU while the kernel runs, so other
+ * work on the device waits until sjbg_eager_end_of_stream stops it or its
+ * wait for the next batch runs out (idle_timeout_ms).  The window state stays
+ * in device memory when the kernel returns; the next batch relaunches it. */
+
+/* Post one batch without waiting; *ticket names it for sjbg_eager_wait.  A host
+ * batch is copied before the call returns; a device batch (16-byte aligned)
+ * is read in place and must stay unchanged until its ticket completes. */
+SJBG_API int sjbg_eager_post(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int is_left, uint32_t mem,
+                             uint64_t *ticket);
+/* Wait for a posted batch (one of the last 64 posted) and return its new
+ * matches.  SJBG_E_TIMEOUT when the kernel does not answer within
+ * idle_timeout_ms + 2 s or one of its bounded device-side waits gave up (the
+ * handle then refuses batches until sjbg_eager_clear_states). */
+SJBG_API int sjbg_eager_wait(sjbg_handle *h, uint64_t ticket, uint64_t *match_count);
+/* Whether the kernel is resident, and how often it was launched.  Returns
+ * SJBG_E_TIMEOUT once after the kernel returned because its wait for the next
+ * batch ran out (its device status word then holds the timeout bit); SJBG_OK
+ * otherwise. */
+SJBG_API int sjbg_eager_pk_status(sjbg_handle *h, int *running, uint64_t *launches);
 
 /* ---- streaming loop (no reference counterpart) --------------------------------
  * Event-time tumbling windows of window_ns, admitted under hbm_budget_bytes. */
