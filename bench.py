@@ -109,16 +109,19 @@ class ClockSampler:
 
 # ---------------------------------------------------------------------------- reference arm
 def run_reference(args, workload):
-    """The reference's CPU joiner for this path on the host cores: the oracle's
-    restatement of lazy CPU_SMJ (CPU_HJ is infeasible at z=1.5: O(sum |L_k||R_k|)
-    bucket compares), one window of the workload per step."""
+    """The reference's CPU joiner for this path on the host cores, one window of
+    the workload per step: the reference's own lazy CPU_SMJ
+    (src/sjb/windowing/lazy/executor/CPU/CPU_SMJ.cpp:23-139) compiled from its
+    sources into oracle/_ref when that library loads here, else the oracle's
+    restatement of it (kind "port").  CPU_HJ is infeasible at z=1.5: O(sum
+    |L_k||R_k|) bucket compares."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
     import oracle_py as O
 
     nwin, W, D, z = WORKLOADS[workload]
     cores = os.cpu_count() or 1
     table = O.zipf_table(D, z) if z is not None else None
+    ref = O.ref_lib() is not None
     per_step = []
     for step in range(args.warmup + args.steps):
         w = step % nwin
@@ -129,18 +132,24 @@ def run_reference(args, workload):
             l = O.gen_uniform(w * W, W, 1, D, cores)
             r = O.gen_uniform(w * W, W, 2, D, cores)
         t0 = time.perf_counter()
-        O.lazy_smj_count(l, r, D, threads=cores)
+        if ref:
+            O.ref_lazy_smj_count(l, r, D, W, cores)
+        else:
+            O.lazy_smj_count(l, r, D, threads=cores)
         dt = time.perf_counter() - t0
         if step >= args.warmup:
             per_step.append(dt)
     value = 2 * W * len(per_step) / sum(per_step)
+    kind = "reference" if ref else "port"
+    what = ("the reference's CPU_SMJ compiled from its sources (oracle/_ref)" if ref else
+            "lazy CPU_SMJ restated (the reference's sources are not on this machine)")
     return {"metric": "joined input tuples/s", "value": value, "unit": "tuples/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(per_step) / len(per_step),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": workload, "sample": f"one window of {W} tuples per stream per step"},
-            "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": cores, "kind": "port",
-                             "sample": f"lazy CPU_SMJ restated, one window of {W} tuples/stream per step"},
+            "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": cores, "kind": kind,
+                             "sample": f"{what}, one window of {W} tuples/stream per step"},
             "e2e": {"value": value, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -395,6 +404,306 @@ def bench_stream(args, sjbg, torch, dev, rate=1e9, seconds=3.0, window_ms=100, c
                   "notes": "real-time paced; Zipf exponent drift compressed to thirds of the run"})
 
 
+# ---------------------------------------------------------------------------- every configuration, one line
+def launch_bytes(kernel, n, light_frac=1.0):
+    """Algorithmic bytes of one launch of `kernel` over n input tuples (both
+    streams).  Hash join: part_hist reads each 16-byte tuple once; part_scatter
+    reads it and writes an 8-byte (key, val) word; bucket joins read those
+    words; HBM-table build / probe read one side's tuples each.  Sort-merge
+    join: sort_extract reads a tuple and writes its key and val; one radix
+    downsweep pass reads and writes 8 bytes per tuple, the upsweep reads the
+    key; merge_join reads the sorted keys and vals."""
+    if kernel == "part_hist":
+        return 16 * n
+    if kernel == "part_scatter":
+        return 16 * n + 8 * n * light_frac
+    if kernel == "part_fine":
+        return 16 * n * light_frac
+    if kernel.startswith("bucket_join"):
+        return 8 * n * light_frac
+    if kernel.startswith("ht_build") or kernel.startswith("ht_probe"):
+        return 8 * n
+    if kernel == "sort_extract":
+        return 24 * n
+    if kernel.startswith("rs_downsweep"):
+        return 16 * n
+    if kernel.startswith("rs_upsweep"):
+        return 4 * n
+    if kernel.startswith("merge_join"):
+        return 8 * n
+    return None
+
+
+def profile_top(torch, j, step, n, peak, light_frac=1.0, reps=3):
+    """Run `step` on a profiling handle (SJBG_F_PROFILE: CUDA events around
+    every launch on the handle's stream) and report the kernel with the most
+    device time: its share of the step, launches, and achieved bytes / launch
+    time against the measured HBM peak."""
+    step()
+    torch.cuda.synchronize()
+    j.kernel_stats_reset()
+    for _ in range(reps):
+        step()
+    torch.cuda.synchronize()
+    stats = j.kernel_stats()
+    if not stats:
+        return None
+    total = sum(v[1] for v in stats.values())
+    name, (launches, ms) = max(stats.items(), key=lambda kv: kv[1][1])
+    per = ms / launches
+    alg = launch_bytes(name, n, light_frac)
+    out = {"kernel": name, "share": ms / total if total else None, "launches_per_step": launches / reps,
+           "launch_ms": per}
+    if alg:
+        gbs = alg / (per * 1e-3) / 1e9
+        out.update(bound="hbm", achieved_gbs=gbs, frac=gbs / peak, algorithmic_bytes_per_launch=alg)
+    return out
+
+
+def eager_windows(n_batches, B, W):
+    """The reference's eager windows (eager/CountBased.cuh:36-72) over batches
+    L0, R0, L1, R1, ...: per window its (left batches, right batches)."""
+    wins, cur, tot = [], ([], []), [0, 0]
+    for b in range(n_batches):
+        for side in (0, 1):
+            if tot[0] >= W or tot[1] >= W:
+                wins.append(cur)
+                cur, tot = ([], []), [0, 0]
+            cur[side].append(b)
+            tot[side] += B
+    wins.append(cur)
+    return wins
+
+
+def suite_uniform(args, sjbg, torch, dev, peak):
+    """Config 1: 16 windows x 65,536 tuples per stream, keys uniform in [0, 65,536)."""
+    nwin, W, D = 16, 65536, 65536
+    total = nwin * W
+    dL = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    dR = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    j = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, flags=sjbg.F_GRAPH, max_tuples_per_window=W, device=dev)
+    j.generate(dL.data_ptr(), 0, total, 1, D)
+    j.generate(dR.data_ptr(), 0, total, 2, D)
+    stream = torch.cuda.Stream()
+    j.set_stream(stream.cuda_stream)
+    descs = (sjbg.WindowDesc * nwin)(*[sjbg.WindowDesc(w * W, W, w * W, W, 0, 0) for w in range(nwin)])
+    res = (sjbg.WindowResult * nwin)()
+    step = lambda jj: jj.lazy_execute_batch_raw(dL.data_ptr(), dR.data_ptr(), descs, res)
+    ms = _events_time(torch, stream, lambda: step(j), args.steps, args.warmup, flush=True)
+    one = (sjbg.WindowDesc * 1)()
+    r1 = (sjbg.WindowResult * 1)()
+    direct = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, max_tuples_per_window=W, device=dev)
+    direct.set_stream(stream.cuda_stream)
+    lat = []
+    for rep in range(3):
+        for w in range(nwin):
+            one[0] = sjbg.WindowDesc(w * W, W, w * W, W, 0, 0)
+            direct.lazy_execute_batch_raw(dL.data_ptr(), dR.data_ptr(), one, r1)
+            if rep:
+                lat.append(r1[0].ms)
+    lat.sort()
+    prof = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, flags=sjbg.F_PROFILE, max_tuples_per_window=W, device=dev)
+    prof.set_stream(stream.cuda_stream)
+    top = profile_top(torch, prof, lambda: step(prof), 2 * total, peak)
+    for x in (j, direct, prof):
+        x.close()
+    return {"value": 2 * total / (ms * 1e-3), "unit": "tuples/s", "ms_per_step": ms,
+            "workload": "16 windows x 65,536 per stream, keys U[0, 65,536), automatic partitioning, graph replay",
+            "l2": "inputs (32 MiB) fit in L2: a 256 MiB write flushes L2 before every timed step",
+            "latency": {"p50_ms": lat[len(lat) // 2], "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                        "unit": "ms per single-window call"},
+            "dominant_kernel": top}
+
+
+def suite_batched(args, sjbg, torch, dev, peak):
+    """Config 4: 1,024 windows, sizes log-uniform in [2^10, 2^20] (seed 4), keys U[0, 4W)."""
+    sizes = [sjbg_log_uniform(w) for w in range(1024)]
+    total = sum(sizes)
+    dl = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    dr = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    hj = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, flags=sjbg.F_GRAPH | sjbg.F_AUTOTUNE, max_tuples_per_window=1 << 20,
+                     device=dev)
+    smj = sjbg.Joiner(sjbg.ALG_SMJ, sjbg.LAZY, flags=sjbg.F_GRAPH, max_tuples_per_window=1 << 20, device=dev)
+    descs_l, off = [], 0
+    for n in sizes:
+        hj.generate(dl.data_ptr() + 16 * off, off, n, 1, 4 * n)
+        hj.generate(dr.data_ptr() + 16 * off, off, n, 2, 4 * n)
+        descs_l.append((off, n, off, n, 0, 0))
+        off += n
+    descs = (sjbg.WindowDesc * 1024)(*[sjbg.WindowDesc(*d) for d in descs_l])
+    res_h, res_s = (sjbg.WindowResult * 1024)(), (sjbg.WindowResult * 1024)()
+    for j in (hj, smj):
+        j.set_stream(stream.cuda_stream)
+    step_h = lambda j: j.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res_h)
+    step_s = lambda j: j.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res_s)
+    ms_h = _events_time(torch, stream, lambda: step_h(hj), args.steps, args.warmup)
+    ms_s = _events_time(torch, stream, lambda: step_s(smj), max(3, args.steps // 2), args.warmup)
+    same = [(a.count, a.prod_checksum) for a in res_h] == [(a.count, a.prod_checksum) for a in res_s]
+    n = 2 * total
+    tops = {}
+    for key, alg, fl in (("hj", sjbg.ALG_HJ, sjbg.F_AUTOTUNE), ("smj", sjbg.ALG_SMJ, 0)):
+        prof = sjbg.Joiner(alg, sjbg.LAZY, flags=sjbg.F_PROFILE | fl, max_tuples_per_window=1 << 20, device=dev)
+        prof.set_stream(stream.cuda_stream)
+        r = (sjbg.WindowResult * 1024)()
+        tops[key] = profile_top(torch, prof, lambda: prof.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(),
+                                                                                 descs, r), n, peak)
+        prof.close()
+    hj.close()
+    smj.close()
+    common = {"workload": "1,024 windows, sizes log-uniform in [2^10, 2^20] per stream (seed 4), keys U[0, 4W), "
+                          "graph replay", "tuples_per_step": n,
+              "l2": f"inputs larger than L2 ({n * 16 >> 20} MiB per step)"}
+    return ({"value": n / (ms_h * 1e-3), "unit": "tuples/s", "ms_per_step": ms_h, "autotuned": True,
+             "dominant_kernel": tops["hj"], **common},
+            {"value": n / (ms_s * 1e-3), "unit": "tuples/s", "ms_per_step": ms_s, "dominant_kernel": tops["smj"],
+             "outputs_identical_to_hash_join": same, **common})
+
+
+def suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, algo, W, D, n_batches):
+    """Config 2, whole recorded stream in one call (sjbg_eager_run): batches of
+    4,096, the reference's close rule."""
+    B = 4096
+    n = n_batches * B
+    dl = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    dr = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    a = sjbg.ALG_SMJ if algo == "SMJ" else sjbg.ALG_NLJ
+    j = sjbg.Joiner(a, sjbg.EAGER, batch_size=B, window_size=W, max_tuples_per_window=W, device=dev)
+    j.generate(dl.data_ptr(), 0, n, 1, D)
+    j.generate(dr.data_ptr(), 0, n, 2, D)
+    stream = torch.cuda.Stream()
+    j.set_stream(stream.cuda_stream)
+    out = {}
+    step = lambda jj: out.__setitem__("r", jj.eager_run(dl, dr, n_batches, mem=sjbg.MEM_DEVICE))
+    ms = _events_time(torch, stream, lambda: step(j), max(3, args.steps // 2), args.warmup, flush=True)
+    bc = out["r"][0]
+    prof = sjbg.Joiner(a, sjbg.EAGER, flags=sjbg.F_PROFILE, batch_size=B, window_size=W, max_tuples_per_window=W,
+                       device=dev)
+    prof.set_stream(stream.cuda_stream)
+    top = profile_top(torch, prof, lambda: step(prof), 2 * n, peak)
+    if algo == "NLJ" and top:
+        # compare-bound: every (left batch, right batch) pair of a window compares B x B keys
+        compares = sum(len(lb) * len(rb) for lb, rb in eager_windows(n_batches, B, W)) * B * B
+        peak_cmp = 152 * 128 * (sm_mhz or 2070.0) * 1e6   # SMs x int32 lanes per SM x clock
+        achieved = compares / (top["launch_ms"] * top["launches_per_step"] * 1e-3)
+        top.update(bound="int-compare", achieved_compares_per_s=achieved, peak_compares_per_s=peak_cmp,
+                   frac=achieved / peak_cmp, peak_kind="152 SMs x 128 int32 lanes x median SM clock")
+    j.close()
+    prof.close()
+    return {"value": 2 * n / (ms * 1e-3), "unit": "tuples/s", "ms_per_step": ms,
+            "workload": f"eager {algo}, window {W}, batches of {B}, {n_batches} batches per side, keys U[0, {D})",
+            "call": "sjbg_eager_run (whole recorded stream)", "matches": int(bc.sum()),
+            "l2": "a 256 MiB write flushes L2 before every timed call", "dominant_kernel": top}
+
+
+def suite_eager_batches(args, sjbg, torch, dev, algo, W, D, n_batches):
+    """Config 2 through the reference's per-batch interface (sjbg_eager_execute,
+    BaseEagerExecutor::execute): pinned host batches of 4,096 as the reference's
+    source delivers them, the close rule applied by the caller.  Per-batch
+    launches (one kernel sequence + a result copy + a stream sync per batch)
+    against the persistent kernel (one resident kernel fed by the ticket
+    queue), synchronous (p50/p99 per-batch latency) and with 32 batches posted
+    ahead."""
+    import numpy as np
+    B = 4096
+    n = n_batches * B
+    a = {"SMJ": sjbg.ALG_SMJ, "NLJ": sjbg.ALG_NLJ, "HJ": sjbg.ALG_HJ}[algo]
+    dl = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    dr = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    g = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, device=dev)
+    g.generate(dl.data_ptr(), 0, n, 1, D)
+    g.generate(dr.data_ptr(), 0, n, 2, D)
+    g.close()
+    hl = torch.empty(n * 16, dtype=torch.uint8, pin_memory=True)
+    hr = torch.empty(n * 16, dtype=torch.uint8, pin_memory=True)
+    hl.copy_(dl)
+    hr.copy_(dr)
+    torch.cuda.synchronize()
+    del dl, dr
+    order = []   # (side, batch), with "clear" markers, in the reference's order
+    tot = [0, 0]
+    for b in range(n_batches):
+        for side in (0, 1):
+            if tot[0] >= W or tot[1] >= W:
+                order.append(None)
+                tot = [0, 0]
+            order.append((side, b))
+            tot[side] += B
+    ptr = [hl.data_ptr(), hr.data_ptr()]
+
+    def run(j, ahead=0):
+        counts, lat, pend = [], [], []
+        j.eager_clear_states()   # a fresh window (the warm-up pass left its last one open)
+        t0 = time.perf_counter()
+        for item in order:
+            if item is None:
+                while pend:
+                    counts.append(j.eager_wait(pend.pop(0)))
+                j.eager_clear_states()
+                continue
+            side, b = item
+            if ahead:
+                pend.append(j.eager_post(ptr[side] + 16 * b * B, side == 0, n=B))
+                if len(pend) >= ahead:
+                    counts.append(j.eager_wait(pend.pop(0)))
+            else:
+                c0 = time.perf_counter()
+                counts.append(j.eager_execute(ptr[side] + 16 * b * B, side == 0, n=B))
+                lat.append(time.perf_counter() - c0)
+        while pend:
+            counts.append(j.eager_wait(pend.pop(0)))
+        wall = time.perf_counter() - t0
+        j.eager_end_of_stream()
+        return counts, wall, lat
+
+    out = {}
+    ref_counts = None
+    for mode, flags, ahead in (("per_batch_launches", 0, 0), ("persistent", sjbg.F_PERSISTENT, 0),
+                               ("persistent_posted_ahead", sjbg.F_PERSISTENT, 32)):
+        j = sjbg.Joiner(a, sjbg.EAGER, flags=flags, batch_size=B, window_size=W, max_tuples_per_window=W,
+                        device=dev)
+        run(j, ahead)   # warm-up pass (allocations, kernel launch)
+        counts, wall, lat = run(j, ahead)
+        j.close()
+        lat.sort()
+        r = {"value": 2 * n / wall, "unit": "tuples/s", "wall_ms": wall * 1e3}
+        if lat:
+            r["latency"] = {"p50_ms": 1e3 * lat[len(lat) // 2], "p99_ms": 1e3 * lat[min(len(lat) - 1,
+                                                                                       int(0.99 * len(lat)))],
+                            "unit": "ms per sjbg_eager_execute call (host wall clock)"}
+        if ref_counts is None:
+            ref_counts = counts
+        r["counts_identical"] = counts == ref_counts
+        out[mode] = r
+    out["workload"] = (f"eager {algo}, window {W}, {n_batches} pinned host batches of {B} per side, "
+                       f"keys U[0, {D}); timed on the host wall clock, H2D inside")
+    out["matches"] = int(np.sum(ref_counts))
+    return out
+
+
+def config_suite(args, sjbg, torch, dev, peak, sm_mhz):
+    """The other configurations, each under the same run's clock."""
+    suite = {}
+    t0 = time.perf_counter()
+    suite["c1_uniform_hj"] = suite_uniform(args, sjbg, torch, dev, peak)
+    suite["c2_eager_smj"] = suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, "SMJ", 1 << 20, 1 << 20, 1024)
+    suite["c2_eager_nlj"] = suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, "NLJ", 65536, 65536, 64)
+    suite["c2_eager_smj_per_batch"] = suite_eager_batches(args, sjbg, torch, dev, "SMJ", 1 << 20, 1 << 20, 300)
+    suite["c2_eager_nlj_per_batch"] = suite_eager_batches(args, sjbg, torch, dev, "NLJ", 65536, 65536, 64)
+    suite["c2_eager_hj_per_batch"] = suite_eager_batches(args, sjbg, torch, dev, "HJ", 1 << 20, 1 << 20, 300)
+    suite["c4_batched_hj"], suite["c4_batched_smj"] = suite_batched(args, sjbg, torch, dev, peak)
+    torch.cuda.empty_cache()
+    st = bench_stream(args, sjbg, torch, dev, rate=1e9)
+    suite["c5_stream_1g"] = {"value": st["value"], "unit": "tuples/s", "wall_ms": st["ms_per_step"],
+                             "latency": st["latency"], "windows": st["windows"], "rejected": st["rejected"],
+                             "fallbacks": st["fallbacks"], "keeps_up": st["keeps_up"],
+                             "workload": "1 G tuples/s offered, Poisson batches of 4,096, 100 ms event-time windows, "
+                                         "Zipf over 2^26 drifting 0.8 -> 1.2 -> 1.5, learned partitioning, "
+                                         "120 GB budget, real-time paced for 3 s"}
+    suite["seconds"] = time.perf_counter() - t0
+    return suite
+
+
 SPECIAL = {
     "batched_1024": bench_batched,
     "eager_smj_2p20": bench_eager_smj,
@@ -459,6 +768,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="skewed_hj_z1.5", choices=sorted(WORKLOADS) + sorted(SPECIAL))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-suite", action="store_true", help="headline workload only (skip the other configurations)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -677,17 +987,21 @@ def main():
         "kernel_ms_per_step": {k: v[1] / 3 for k, v in stats.items()},
         "clocks": clocks.summary(),
     }
+    learned.close()
+    plain.close()
+    radix_auto.close()
+    hbm_table.close()
+    direct.close()
+    del dL, dR, hL, hR
+    torch.cuda.empty_cache()
+    if not args.no_suite and args.workload == "skewed_hj_z1.5" and world == 1:
+        out["configs"] = config_suite(args, sjbg, torch, local, peak, out["clocks"].get("sm_mhz"))
     if not args.no_cpu_baseline and rank == 0:
         ref_args = argparse.Namespace(gpus=1, steps=1, warmup=0)
         cb = run_reference(ref_args, args.workload)
         out["cpu_baseline"] = dict(cb["cpu_baseline"])
     if rank == 0:
         print(json.dumps(out))
-    learned.close()
-    plain.close()
-    radix_auto.close()
-    hbm_table.close()
-    direct.close()
 
 
 if __name__ == "__main__":

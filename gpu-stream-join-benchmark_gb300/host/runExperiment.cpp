@@ -10,7 +10,9 @@
 // Optional keys with no reference counterpart: dataSize (tuples per stream,
 // default 2560 MiB of tuples), sourceThreads (default 32), tsUpperBound
 // (default 1000), gpuDevice (CUDA device of the joiners and of the power
-// sampler, default 0).  --list prints the expanded configurations and their
+// sampler, default 0), usePK ("Yes" / "No", default "No": the reference's
+// EagerJoinConfig::usePK, include/experiment/Config.hpp:15 - eager joiners
+// run as one persistent kernel fed by a queue).  --list prints the expanded configurations and their
 // algorithm names without touching a GPU.
 #include <cuda_runtime.h>
 
@@ -138,8 +140,8 @@ std::pair<std::string, uint64_t> runExperimentWithConfig(const ExperimentConfig 
         LOG_INFO("Joiner: %s, Match Count: %lu, Selectivity: %.6f%%, ElapsedTime: %lu ms",
                  windowing->getAlgorithmName().c_str(), (unsigned long)matchCount, selectivity,
                  (unsigned long)msElapsed);
-        LOG_INFO("Windows: %lu, Prod checksum: %lu", (unsigned long)sink.getExecutedWindows(),
-                 (unsigned long)sink.prodChecksum);
+        LOG_INFO("Windows: %lu, Prod checksum: %lu, Window pairs: %lu", (unsigned long)sink.getExecutedWindows(),
+                 (unsigned long)sink.prodChecksum, (unsigned long)sink.getWindowPairs());
         LOG_INFO("Avg Build: %lu, Avg Probe: %lu", (unsigned long)sink.getAverageBuildTime(),
                  (unsigned long)sink.getAverageProbeTime());
         LOG_INFO("Avg Sort: %lu, Avg Merge: %lu", (unsigned long)sink.getAverageSortTime(),
@@ -299,6 +301,11 @@ int main(int argc, char **argv) {
         if (y.has("sourceThreads")) ec.sourceThreads = std::stoull(y.scalar("sourceThreads"));
         if (y.has("tsUpperBound")) ec.dataConfig.timestampUpperBound = std::stoull(y.scalar("tsUpperBound"));
         if (y.has("gpuDevice")) ec.engineConfig.gpuDevice = std::stoi(y.scalar("gpuDevice"));
+        if (y.has("usePK")) {
+            const std::string pk = y.scalar("usePK");
+            if (pk != "Yes" && pk != "No") throw std::invalid_argument("Unknown parameter for usePK: " + pk);
+            ec.algorithmConfig.eagerJoinConfig.usePK = pk == "Yes";
+        }
         const std::string metric = y.scalar("measuredMetric");
         if (metric != "Throughput" && metric != "cumulativePercentage")
             throw std::invalid_argument("Unknown measured metrics: " + metric);

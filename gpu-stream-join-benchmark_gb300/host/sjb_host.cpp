@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cctype>
 #include <condition_variable>
@@ -166,21 +167,32 @@ CountBased::CountBased(Sink &sink, uint64_t ringBufferSize, uint64_t ringBufferM
         available[1].push_back(i * batchSize);
     }
     // Pinned, as the reference's ring (include/sjb/windowing/lazy/CountBased.cuh:35-36), so the
-    // joiners' host-to-device copies of a window's batches run at the link's rate.
-    for (int s = 0; s < 2; s++) {
-        void *p = nullptr;
-        if (cudaMallocHost(&p, sizeof(Tuple) * ringBufferSize) != cudaSuccess) {
-            cudaGetLastError();
-            if (ring[0]) cudaFreeHost(ring[0]);
-            throw std::runtime_error("CountBased: cudaMallocHost of the ring buffer failed");
+    // joiners' host-to-device copies of a window's batches run at the link's rate.  Without a
+    // CUDA device (executors that are not GPU joiners) the ring is plain host memory.
+    void *p0 = nullptr, *p1 = nullptr;
+    ringPinned = cudaMallocHost(&p0, sizeof(Tuple) * ringBufferSize) == cudaSuccess &&
+                 cudaMallocHost(&p1, sizeof(Tuple) * ringBufferSize) == cudaSuccess;
+    if (!ringPinned) {
+        cudaGetLastError();
+        if (p0) cudaFreeHost(p0);
+        p0 = std::malloc(sizeof(Tuple) * ringBufferSize);
+        p1 = std::malloc(sizeof(Tuple) * ringBufferSize);
+        if (!p0 || !p1) {
+            std::free(p0);
+            std::free(p1);
+            throw std::runtime_error("CountBased: the ring buffer could not be allocated");
         }
-        ring[s] = static_cast<Tuple *>(p);
     }
+    ring[0] = static_cast<Tuple *>(p0);
+    ring[1] = static_cast<Tuple *>(p1);
 }
 
 CountBased::~CountBased() {
-    for (Tuple *r : ring)
-        if (r) cudaFreeHost(r);
+    for (Tuple *r : ring) {
+        if (!r) continue;
+        if (ringPinned) cudaFreeHost(r);
+        else std::free(r);
+    }
 }
 
 void CountBased::incoming(Tuple *batch, int side) {
@@ -262,6 +274,7 @@ void CountBased::harvestChecksums() {
     if (auto *gpu = dynamic_cast<Executor::GPUJoinEagerExecutor *>(joiner.get())) {
         const sjbg_window_result r = gpu->windowResult();
         sink.addChecksums(r.xor_checksum, r.prod_checksum);
+        sink.addWindowPairs(r.count);
     }
 }
 
@@ -324,10 +337,10 @@ std::string WindowingFactory::algorithmName(const AlgorithmConfig &a) {
     // Bitmap materialisation exists for the nested-loop join only, as in the reference.
     if (a.resultWritingMethod == RESULT_WRITING_METHOD::Bitmap && a.underlyingAlgorithm != ALGORITHM_TYPE::NLJ)
         throw std::runtime_error("Not Implemented");
-    if (a.progressiveness == PROGRESSIVENESS_TYPE::EAGER && a.eagerJoinConfig.usePK)
-        throw std::runtime_error("Not Implemented");
     std::string name = a.progressiveness == PROGRESSIVENESS_TYPE::LAZY ? "lazy_gpu_" : "eager_gpu_";
-    return name + alg + "_" + res;
+    // eager joiners as one persistent kernel (the reference's usePK; its GPU_HJ_PK has no factory name)
+    const bool pk = a.progressiveness == PROGRESSIVENESS_TYPE::EAGER && a.eagerJoinConfig.usePK;
+    return name + alg + (pk ? "_pk_" : "_") + res;
 }
 
 sjbg_config WindowingFactory::toConfig(const AlgorithmConfig &a, const DataConfig &d, const QueryConfig &q,
@@ -342,6 +355,8 @@ sjbg_config WindowingFactory::toConfig(const AlgorithmConfig &a, const DataConfi
     c.window_size = q.windowSize;
     c.num_distinct_keys = d.numDistinctKey;
     c.device = e.gpuDevice;
+    // the reference's EagerJoinConfig::usePK (persistent kernels) for eager executors
+    if (a.progressiveness == Windowing::EAGER && a.eagerJoinConfig.usePK) c.flags |= SJBG_F_PERSISTENT;
     return c;
 }
 

@@ -65,6 +65,11 @@ public:
     void addToCounter(uint64_t m, bool closed);
     void addToPossibleMatches(uint64_t c) { possible += c; }
     void addToExecutedWindows(uint64_t c) { windows += c; }
+    // Matches of closed eager windows, from each window's own totals (no
+    // reference counterpart): equal to getMatchCount(), the sum of the batch
+    // counts, when every batch is counted into the window it joined.
+    void addWindowPairs(uint64_t c) { windowPairs += c; }
+    uint64_t getWindowPairs() const { return windowPairs; }
     void addChecksums(uint64_t xr, uint64_t prod) {
         std::lock_guard<std::mutex> g(mu);
         xorChecksum ^= xr;
@@ -92,7 +97,7 @@ public:
     uint64_t xorChecksum = 0, prodChecksum = 0;
 
 private:
-    std::atomic<uint64_t> counter{0}, possible{0}, windows{0};
+    std::atomic<uint64_t> counter{0}, possible{0}, windows{0}, windowPairs{0};
     std::atomic<uint64_t> buildTime{0}, probeTime{0}, sortTime{0}, mergeTime{0};
     std::chrono::time_point<std::chrono::high_resolution_clock> start = std::chrono::high_resolution_clock::now();
     mutable std::mutex mu;
@@ -220,6 +225,7 @@ private:
     uint64_t ringBufferSize, ringBufferMaxTries, windowSize, batchSize;
     std::unique_ptr<Impl> impl;
     Tuple *ring[2] = {nullptr, nullptr};   // pinned host memory (cudaMallocHost), as the reference's
+    bool ringPinned = false;               // false: no CUDA device, plain host memory
     std::deque<uint64_t> available[2], executable[2];
     std::mutex mu;
 };

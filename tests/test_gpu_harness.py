@@ -17,13 +17,14 @@ B = 1 << 13            # batchSizeKB: [128]
 DISTINCT = 1000
 
 
-def run(harness, tmp_path, alg, prog, result="NoOutput", theta="0.0", distinct=DISTINCT, power="No"):
+def run(harness, tmp_path, alg, prog, result="NoOutput", theta="0.0", distinct=DISTINCT, power="No", extra=""):
     y = tmp_path / "exp.yaml"
     y.write_text(
         f'algTypes: [ "{alg}" ]\ndeviceTypes: [ "GPU" ]\nprogressivenessModes: [ "{prog}" ]\n'
         f"distinctKeys: [ {distinct} ]\nzipfThetas: [ {theta} ]\nresultMaterializationMethod: [ \"{result}\" ]\n"
         f'windowSizesMB: [ 1 ]\nbatchSizeKB: [ 128 ]\nmeasuredMetric: "cumulativePercentage"\n'
-        f'measurePowerUsage: "{power}"\nrepeat: 1\nparStrats: [ "INTRA" ]\ndataSize: {N}\nsourceThreads: 1\n')
+        f'measurePowerUsage: "{power}"\nrepeat: 1\nparStrats: [ "INTRA" ]\ndataSize: {N}\n'
+        + (extra if "sourceThreads" in extra else extra + "sourceThreads: 1\n"))
     r = subprocess.run([harness, str(y), str(tmp_path / "out.csv")], capture_output=True, text=True,
                        cwd=tmp_path, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -31,6 +32,7 @@ def run(harness, tmp_path, alg, prog, result="NoOutput", theta="0.0", distinct=D
     m = re.search(r"Match Count: (\d+)", r.stdout)
     p = re.search(r"Prod checksum: (\d+)", r.stdout)
     w = re.search(r"Windows: (\d+)", r.stdout)
+    run.window_pairs = int(re.search(r"Window pairs: (\d+)", r.stdout).group(1))
     rows = (tmp_path / "progressiveness.csv").read_text().strip().splitlines()[1:]
     progress = [int(row.split(",")[4]) for row in rows]
     return int(m.group(1)), int(p.group(1)), int(w.group(1)), progress
@@ -76,14 +78,28 @@ def test_lazy_harness_zipf(harness, oracle, tmp_path):
     assert prod == sum(r["prod"] for r in want) % (1 << 64)
 
 
-@pytest.mark.parametrize("alg", ["HJ", "NLJ"])
-def test_eager_harness_matches_oracle(harness, oracle, tmp_path, alg):
+@pytest.mark.parametrize("alg,pk", [("HJ", "No"), ("NLJ", "No"), ("HJ", "Yes"), ("NLJ", "Yes"), ("SMJ", "Yes")])
+def test_eager_harness_matches_oracle(harness, oracle, tmp_path, alg, pk):
+    """usePK: "Yes" runs the eager joiner as one persistent kernel."""
     left, right = streams(oracle)
-    count, _, windows, progress = run(harness, tmp_path, alg, "EAGER")
+    count, _, windows, progress = run(harness, tmp_path, alg, "EAGER", extra=f'usePK: "{pk}"\n')
     bc, wc = oracle.eager_hj(left, right, B, W, DISTINCT)
     assert count == int(bc.sum())
     assert progress == np.cumsum(bc).tolist()          # one progress record per batch, arrival order
     assert windows == len(wc) - 1                      # closes counted; the last window stays open
+
+
+@pytest.mark.parametrize("pk", ["No", "Yes"])
+def test_eager_harness_eight_source_threads(harness, tmp_path, pk):
+    """Eight source threads deliver batches concurrently.  The order differs
+    from run to run, but each batch is executed and counted in the window it
+    joined: the sum of the batch counts equals the sum of the windows' own
+    totals, and every tuple is accounted for."""
+    count, _, windows, progress = run(harness, tmp_path, "HJ", "EAGER",
+                                      extra=f'usePK: "{pk}"\nsourceThreads: 8\n')
+    assert count == run.window_pairs > 0
+    assert len(progress) == 2 * N // B and progress[-1] == count
+    assert windows >= N // W - 1
 
 
 def test_power_samples_written(harness, tmp_path):

@@ -103,3 +103,55 @@ def test_bad_files_fail(harness, tmp_path, key, value, msg):
 def test_usage_message(harness):
     r = subprocess.run([harness], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "runExperiment <path_to_yaml_config> <outputFileName>" in r.stdout
+
+
+def test_use_pk_key(harness, tmp_path):
+    rc, rows, _ = listing(harness, write_yaml(tmp_path, usePK='"Yes"', progressivenessModes='[ "EAGER" ]'))
+    assert rc == 0 and rows[0].split(",")[0] == "eager_gpu_hj_pk_nm"
+    rc, _, err = listing(harness, write_yaml(tmp_path, usePK='"Sometimes"'))
+    assert rc == 2 and "Unknown parameter for usePK: Sometimes" in err
+
+
+@pytest.fixture(scope="module")
+def host_units(tmp_path_factory):
+    """tests/host_units.cpp linked with the host windowing (CPU stand-in executors)."""
+    import os
+    import shutil
+
+    import build as b
+
+    b.build_lib()
+    exe = str(tmp_path_factory.mktemp("units") / "host_units")
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(b.nvcc())))
+    here = os.path.dirname(os.path.abspath(__file__))
+    cmd = [shutil.which("g++") or "g++", "-O1", "-std=c++17", "-I", os.path.join(b.ROOT, "include"), "-I", b.HOST,
+           "-I", os.path.join(cuda, "include"), os.path.join(here, "host_units.cpp"),
+           os.path.join(b.HOST, "sjb_host.cpp"), "-o", exe, "-L", b.LIBDIR, "-lsjbg", "-Wl,-rpath," + b.LIBDIR,
+           "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(cuda, "lib64"),
+           "-lpthread", "-ldl"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def _units(exe, mode):
+    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return dict(line.split("=", 1) for line in r.stdout.strip().splitlines())
+
+
+def test_lazy_ring_buffer_full_is_an_error_and_the_windowing_goes_on(host_units):
+    """With every batch slot held by a window being joined, the next batch
+    fails with the reference's message instead of exiting the process; once
+    the join returns the next window goes through."""
+    out = _units(host_units, "ring")
+    assert out["ring_full_thrown"] == "1" and out["message"] == "Ring buffer is full"
+    assert out["windows"] == "2" and int(out["match_count"]) == 2 * (2 * 1000 + 2)
+
+
+def test_eager_close_rule_under_eight_source_threads(host_units):
+    """Eight source threads: the executor is never entered twice at once, and
+    every batch's matches are counted into the window it joined."""
+    out = _units(host_units, "eager")
+    assert out["overlap"] == "0"
+    assert out["match_count"] == out["window_total"] and int(out["match_count"]) > 0
+    assert out["windows_closed"] == out["sink_windows"] and int(out["windows_closed"]) > 30
