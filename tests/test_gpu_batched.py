@@ -68,30 +68,55 @@ def test_learned_graph_replay_reruns_every_kernel(lib, oracle):
     assert per_replay >= 10 and counts[1] - counts[0] == per_replay
 
 
-def test_batched_1024_windows_hash_equals_sort_merge(lib, oracle):
-    """The 1,024-window shape (sizes log-uniform in [2^10, 2^20], keys in [0, 4W)):
-    two independent joins agree on every window, and sampled windows equal the oracle."""
+@pytest.fixture(scope="module")
+def batched_1024(lib, oracle):
+    """The 1,024-window shape (sizes log-uniform in [2^10, 2^20] per stream,
+    seed 4; keys in [0, 4W)), generated on the device, and the oracle's count,
+    xor checksum and prod of every window (about W/4 pairs per window, all
+    enumerated)."""
     torch = pytest.importorskip("torch")
     sizes = [oracle.log_uniform(4, w, 1 << 10, 1 << 20) for w in range(1024)]
     total = sum(sizes)
     dl = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
     dr = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
     descs, off = [], 0
-    with lib.Joiner(lib.ALG_HJ, lib.LAZY, flags=lib.F_GRAPH, max_tuples_per_window=1 << 20) as hj, \
-            lib.Joiner(lib.ALG_SMJ, lib.LAZY, flags=lib.F_GRAPH, max_tuples_per_window=1 << 20) as smj:
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, max_tuples_per_window=1 << 20) as g:
         for n in sizes:
-            hj.generate(dl.data_ptr() + 16 * off, off, n, 1, 4 * n)
-            hj.generate(dr.data_ptr() + 16 * off, off, n, 2, 4 * n)
+            g.generate(dl.data_ptr() + 16 * off, off, n, 1, 4 * n)
+            g.generate(dr.data_ptr() + 16 * off, off, n, 2, 4 * n)
             descs.append((off, n, off, n, 0, 0))
             off += n
-        a = hj.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE)
-        b = smj.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE)
-        a2 = hj.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE)
-    assert [(x["count"], x["prod"]) for x in a] == [(x["count"], x["prod"]) for x in b] == \
-        [(x["count"], x["prod"]) for x in a2]
+    torch.cuda.synchronize()
     hl = dl.cpu().numpy().view(lib.TUPLE_DTYPE)
     hr = dr.cpu().numpy().view(lib.TUPLE_DTYPE)
-    for w in (0, 1, 511, 1023):
-        o, n = descs[w][0], descs[w][1]
-        want = oracle.join(hl[o:o + n], hr[o:o + n], enumerate_pairs=False)
-        assert (a[w]["count"], a[w]["prod"]) == (want["count"], want["prod"])
+    want, _ = oracle.join_windows(hl, hr, descs, enumerate_pairs=True, threads=os.cpu_count() or 8)
+    return dl, dr, descs, want
+
+
+@pytest.mark.parametrize("algo", ["HJ", "SMJ"])
+def test_batched_1024_windows_match_oracle(lib, batched_1024, algo):
+    """Every one of the 1,024 windows, first run and CUDA-graph replay: count,
+    xor checksum (every pair enumerated) and prod equal the oracle's."""
+    dl, dr, descs, want = batched_1024
+    a = lib.ALG_HJ if algo == "HJ" else lib.ALG_SMJ
+    with lib.Joiner(a, lib.LAZY, flags=lib.F_XOR | lib.F_GRAPH, max_tuples_per_window=1 << 20) as j:
+        first = j.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE)
+        again = j.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE)
+    exp = [(w["count"], w["xor"], w["prod"]) for w in want]
+    assert [(g["count"], g["xor"], g["prod"]) for g in first] == exp
+    assert [(g["count"], g["xor"], g["prod"]) for g in again] == exp
+    assert all(g["status"] == 0 for g in first)
+    assert sum(w["count"] for w in want) > 1024 * 256   # about W/4 pairs per window
+
+
+def test_batched_1024_windows_count_only_paths(lib, batched_1024):
+    """Without pair enumeration (count and prod only) the automatic hash join,
+    radix partitioning, learned partitioning and the sort-merge join all equal
+    the oracle on every window."""
+    dl, dr, descs, want = batched_1024
+    exp = [(w["count"], w["prod"]) for w in want]
+    for a, part in ((lib.ALG_HJ, lib.PART_AUTO), (lib.ALG_HJ, lib.PART_RADIX), (lib.ALG_HJ, lib.PART_LEARNED),
+                    (lib.ALG_SMJ, lib.PART_AUTO)):
+        with lib.Joiner(a, lib.LAZY, partitioner=part, max_tuples_per_window=1 << 20) as j:
+            got = j.lazy_execute_batch(dl, dr, descs, mem=lib.MEM_DEVICE)
+        assert [(g["count"], g["prod"]) for g in got] == exp, (a, part)

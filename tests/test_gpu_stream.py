@@ -87,3 +87,67 @@ def test_stream_requires_ordered_event_time(lib):
         back["ts"] = [1, 2, 3, 4]
         with pytest.raises(lib.SjbgError):
             j.stream_push(back, True)
+
+
+def test_stream_full_scale_windows_match_oracle(lib, oracle):
+    """The streaming workload at full scale: two streams at 1 G tuples/s
+    together (Poisson batches of 4,096 per stream), 100 ms event-time windows
+    (about 10^8 tuples each), keys Zipf over [0, 2^26) ranked through the
+    seeded permutation, the exponent stepping 0.8 -> 1.2 -> 1.5 (two windows
+    each here; the workload steps every 10 s), learned partitioning refitted
+    on every window, 120 GB budget.  Generated on the device, pushed in event
+    time order, copied back; every window's count and prod equal the
+    oracle's join of that window's tuples."""
+    import os
+
+    torch = pytest.importorskip("torch")
+    D, B, W_NS, n_win = 1 << 26, 4096, 100_000_000, 6
+    zs = [0.8, 0.8, 1.2, 1.2, 1.5, 1.5]
+    gap_ns = B / 0.5e9 * 1e9          # 0.5 G tuples/s per stream
+    rng = np.random.default_rng(17)
+    tables = {z: torch.from_numpy(lib.zipf_table(D, z).view(np.int64)).cuda() for z in set(zs)}
+    bufs, times = [], []
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, max_tuples_per_window=1 << 30,
+                    hbm_budget_bytes=120 << 30) as j:
+        for side in (0, 1):
+            t = np.cumsum(rng.exponential(gap_ns, int(1.1 * n_win * W_NS / gap_ns)))
+            t = t[t < n_win * W_NS].astype(np.int64)
+            buf = torch.empty(len(t) * B * 16, dtype=torch.uint8, device="cuda")
+            wid = t // W_NS
+            for k in range(n_win):   # each window's batches, with that window's exponent
+                a, b = int(np.searchsorted(wid, k)), int(np.searchsorted(wid, k + 1))
+                j.generate(buf.data_ptr() + 16 * a * B, a * B, (b - a) * B, 1 + side, D,
+                           tables[zs[k]].data_ptr(), 3)
+            buf.view(torch.int64).view(-1, 2)[:, 1] = torch.from_numpy(t).cuda().repeat_interleave(B)
+            bufs.append(buf)
+            times.append(t)
+        torch.cuda.synchronize()
+        j.stream_open(W_NS)
+        results, nxt, step = [], [0, 0], 256   # 256 batches (1 Mi tuples) per push
+        while nxt[0] < len(times[0]) or nxt[1] < len(times[1]):
+            side = 0 if nxt[1] >= len(times[1]) or (nxt[0] < len(times[0]) and
+                                                    times[0][nxt[0]] <= times[1][nxt[1]]) else 1
+            a = int(nxt[side])
+            b = int(min(a + step, len(times[side])))
+            j.stream_push(bufs[side].data_ptr() + 16 * a * B, side == 0, mem=lib.MEM_DEVICE, n=(b - a) * B)
+            nxt[side] = b
+            results += j.stream_poll()
+        stats = j.stream_close()
+        results += j.stream_poll()
+    assert stats["windows_closed"] == n_win and stats["windows_rejected"] == 0
+    hl = bufs[0].cpu().numpy().view(lib.TUPLE_DTYPE)
+    hr = bufs[1].cpu().numpy().view(lib.TUPLE_DTYPE)
+    del bufs
+    descs = []
+    for k in range(n_win):
+        la, lb = np.searchsorted(times[0] // W_NS, [k, k + 1]) * B
+        ra, rb = np.searchsorted(times[1] // W_NS, [k, k + 1]) * B
+        descs.append((int(la), int(lb - la), int(ra), int(rb - ra), 0, 0))
+    want, _ = oracle.join_windows(hl, hr, descs, enumerate_pairs=False, threads=min(n_win, os.cpu_count() or 1))
+    by_id = {r["window_id"]: r for r in results}
+    for k in range(n_win):
+        got = by_id[k]
+        assert got["status"] == 0
+        assert (got["n_left"], got["n_right"]) == (descs[k][1], descs[k][3])
+        assert (got["count"], got["prod"]) == (want[k]["count"], want[k]["prod"]), k
+        assert descs[k][1] + descs[k][3] > 9 * 10 ** 7   # about 10^8 tuples per window
