@@ -681,11 +681,50 @@ def suite_eager_batches(args, sjbg, torch, dev, algo, W, D, n_batches):
     return out
 
 
+def suite_skewed(args, sjbg, torch, dev, z):
+    """Config 3 at another exponent: 8 windows x 2^24 per stream, Zipf(z) over
+    [0, 2^24), ranks permuted (seed 3).  Learned partitioning, radix 2^10, and
+    the one-leaf learned pipeline (heavy-key set, light tuples by key range)."""
+    import numpy as np
+    nwin, W, D = 8, 1 << 24, 1 << 24
+    total = nwin * W
+    dL = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    dR = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    dT = torch.from_numpy(sjbg.zipf_table(D, z).view(np.int64)).cuda()
+    common = dict(algorithm=sjbg.ALG_HJ, progressiveness=sjbg.LAZY, max_tuples_per_window=W, device=dev)
+    g = sjbg.Joiner(**common)
+    g.generate(dL.data_ptr(), 0, total, 1, D, dT.data_ptr(), 3)
+    g.generate(dR.data_ptr(), 0, total, 2, D, dT.data_ptr(), 3)
+    g.close()
+    stream = torch.cuda.Stream()
+    descs = (sjbg.WindowDesc * nwin)(*[sjbg.WindowDesc(w * W, W, w * W, W, 0, 0) for w in range(nwin)])
+    out, results = {}, {}
+    for key, kw in (("learned", dict(partitioner=sjbg.PART_LEARNED)),
+                    ("plain_radix_2p10", dict(partitioner=sjbg.PART_RADIX, radix_bits=10)),
+                    ("heavy_set_radix_light", dict(partitioner=sjbg.PART_LEARNED, learned_leaves=1))):
+        j = sjbg.Joiner(flags=sjbg.F_GRAPH, **kw, **common)
+        j.set_stream(stream.cuda_stream)
+        res = (sjbg.WindowResult * nwin)()
+        ms = _events_time(torch, stream, lambda: j.lazy_execute_batch_raw(dL.data_ptr(), dR.data_ptr(), descs, res),
+                          args.steps, args.warmup)
+        results[key] = [(r.count, r.prod_checksum) for r in res]
+        out[key] = {"value": 2 * total / (ms * 1e-3), "ms_per_step": ms,
+                    "learned_windows": sum(1 for r in res if r.partitioner_used == sjbg.PART_LEARNED)}
+        j.close()
+    out["learned_over_plain"] = out["plain_radix_2p10"]["ms_per_step"] / out["learned"]["ms_per_step"]
+    out["learned_over_radix_heavy"] = out["heavy_set_radix_light"]["ms_per_step"] / out["learned"]["ms_per_step"]
+    out["outputs_identical"] = results["learned"] == results["plain_radix_2p10"] == results["heavy_set_radix_light"]
+    out["workload"] = f"8 windows x 2^24 per stream, Zipf z={z} over [0, 2^24), graph replay, inputs > L2"
+    return out
+
+
 def config_suite(args, sjbg, torch, dev, peak, sm_mhz):
     """The other configurations, each under the same run's clock."""
     suite = {}
     t0 = time.perf_counter()
     suite["c1_uniform_hj"] = suite_uniform(args, sjbg, torch, dev, peak)
+    suite["c3_skewed_z1.0"] = suite_skewed(args, sjbg, torch, dev, 1.0)
+    suite["c3_skewed_z0.5"] = suite_skewed(args, sjbg, torch, dev, 0.5)
     suite["c2_eager_smj"] = suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, "SMJ", 1 << 20, 1 << 20, 1024)
     suite["c2_eager_nlj"] = suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, "NLJ", 65536, 65536, 64)
     suite["c2_eager_smj_per_batch"] = suite_eager_batches(args, sjbg, torch, dev, "SMJ", 1 << 20, 1 << 20, 300)
@@ -831,9 +870,13 @@ def main():
     plain = sjbg.Joiner(partitioner=sjbg.PART_RADIX, radix_bits=plain_bits, flags=sjbg.F_GRAPH, **flags_common)
     radix_auto = sjbg.Joiner(partitioner=sjbg.PART_RADIX, flags=sjbg.F_GRAPH, **flags_common)
     hbm_table = sjbg.Joiner(partitioner=sjbg.PART_NONE, flags=sjbg.F_GRAPH, **flags_common)
+    # the learned pipeline with a one-leaf model: the same sample, heavy-key set
+    # and compaction, light tuples bucketed by one line over their key range
+    # (radix by key range) - what the fitted leaves add is the difference
+    one_leaf = sjbg.Joiner(partitioner=primary_part, learned_leaves=1, flags=sjbg.F_GRAPH, **flags_common)
     direct = sjbg.Joiner(partitioner=primary_part, **flags_common)
     stream = torch.cuda.Stream()
-    for j in (learned, plain, radix_auto, hbm_table, direct):
+    for j in (learned, plain, radix_auto, hbm_table, one_leaf, direct):
         j.set_stream(stream.cuda_stream)
 
     def run_steps(j, k, res):
@@ -880,8 +923,10 @@ def main():
     ms_plain, res_plain = timed(plain, args.steps)
     ms_radix_auto, res_radix_auto = timed(radix_auto, args.steps)
     ms_hbm, res_hbm = timed(hbm_table, args.steps)
+    ms_one, res_one = timed(one_leaf, args.steps)
     same = ([(a[0], a[1]) for a in res_learned] == [(b[0], b[1]) for b in res_plain]
-            == [(b[0], b[1]) for b in res_radix_auto] == [(b[0], b[1]) for b in res_hbm])
+            == [(b[0], b[1]) for b in res_radix_auto] == [(b[0], b[1]) for b in res_hbm]
+            == [(b[0], b[1]) for b in res_one])
 
     # ---- per-window latency (single-window calls, device time per call)
     lat = []
@@ -969,7 +1014,11 @@ def main():
         "radix_same_fanout_as_learned": {"value": tuples / (ms_radix_auto * 1e-3), "ms_per_step": ms_radix_auto},
         "hbm_table": {"value": tuples / (ms_hbm * 1e-3), "ms_per_step": ms_hbm,
                       "partitioner": "none: one open-addressing table per window in HBM"},
+        "heavy_set_radix_light": {"value": tuples / (ms_one * 1e-3), "ms_per_step": ms_one,
+                                  "partitioner": "learned pipeline with a one-leaf model: heavy-key set and "
+                                                 "compaction as learned, light tuples by key range (radix)"},
         "learned_over_plain": ms_plain / ms_learned,
+        "learned_over_radix_heavy": ms_one / ms_learned,
         "learned_windows": sum(1 for a in res_learned if a[2] == sjbg.PART_LEARNED),
         "radix_by_cost_windows": sum(1 for a in res_learned if a[3] & sjbg.WR_RADIX_BY_COST),
         "outputs_identical_learned_vs_plain": same,   # and vs radix (learned fan-out) and the HBM table
@@ -991,6 +1040,7 @@ def main():
     plain.close()
     radix_auto.close()
     hbm_table.close()
+    one_leaf.close()
     direct.close()
     del dL, dR, hL, hR
     torch.cuda.empty_cache()

@@ -693,7 +693,7 @@ __device__ __forceinline__ void scatter_tile(const WorkItem it, const sjbg_tuple
     }
 }
 
-__global__ void __launch_bounds__(kPartThreads, 3)
+__global__ void __launch_bounds__(kPartThreads, 2)
 part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                     uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
                     const uint32_t *__restrict__ workL, const uint32_t *__restrict__ workR,
@@ -1016,6 +1016,129 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
     flush_acc(&acc[bucket_win[b]], count, 0, prod);
 }
 
+// ---- direct-addressed bucket join (radix windows)
+// In a radix window every key of bucket b has key & (2^lg - 1) == b, so key >> lg
+// tells the bucket's keys apart.  When those indices span few values the
+// build side is a direct table {count, sum of fr} indexed by key >> lg: an
+// insert is three shared atomics and a probe two loads, with no key compares
+// or probe loop (the hash table spends about 120 thread instructions per tuple
+// there, and is issue- and shared-memory-bound).  A pass covers kDirectMax
+// indices; a bucket whose indices need more than kDirectPasses passes is left
+// to the hash table, decided after the first build pass and before anything is
+// counted.  Measured on 1,024 uneven windows (keys in [0, 4W), about 4,096
+// left tuples per bucket, two passes): the bucket joins take 2.02 ms, against
+// 2.91 ms with hash tables.
+constexpr uint32_t kDirectMax = 8192;
+constexpr uint32_t kDirectPasses = 2;
+// Larger buckets (a radix window's hot keys) keep the hash table: every extra
+// pass and the table reset re-read the bucket, which one CTA would do serially.
+constexpr uint32_t kDirectMaxRun = 32768;
+constexpr size_t kDirectBytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * kDirectMax;
+
+// `clean`: the leading table entries known to be zero (CTA-uniform); a direct
+// bucket leaves the table zero again, a hash-table bucket does not.  Returns
+// false when the bucket's key range is too wide (the table is left zero).
+__device__ __forceinline__ bool join_count_direct(uint32_t b, const uint64_t *__restrict__ partL,
+                                                  const uint64_t *__restrict__ partR,
+                                                  const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt,
+                                                  uint32_t B, const uint32_t *__restrict__ bucket_win,
+                                                  WinAcc *__restrict__ acc, uint32_t lg, uint32_t &clean) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ uint32_t maxidx_s;
+    const uint32_t nR = cnt[b], nS = cnt[B + b];
+    if (nR == 0 || nS == 0) return true;
+    unsigned long long *dsum = reinterpret_cast<unsigned long long *>(smem_raw);
+    uint32_t *dcnt = reinterpret_cast<uint32_t *>(dsum + kDirectMax);
+    const uint64_t *Rb = partL + start[b];
+    const uint64_t *Sb = partR + start[B + b];
+    for (uint32_t i = clean + threadIdx.x; i < kDirectMax; i += blockDim.x) {
+        dsum[i] = 0;
+        dcnt[i] = 0;
+    }
+    clean = kDirectMax;
+    if (threadIdx.x == 0) maxidx_s = 0;
+    SJBG_BARRIER();
+    const uint32_t tile = kJoinPer * blockDim.x;
+    unsigned long long count = 0, prod = 0;
+    uint32_t passes = 1;
+    for (uint32_t p = 0; p < passes; p++) {
+        const uint32_t lo = p * kDirectMax;
+        uint32_t tmax = 0;
+        // build: the left keys whose index falls in [lo, lo + kDirectMax)
+        for (uint32_t base = 0; base < nR; base += tile) {
+            uint64_t e[kJoinPer];
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t i = base + k * blockDim.x + threadIdx.x;
+                e[k] = i < nR ? Rb[i] : 0ull;
+            }
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                if (base + k * blockDim.x + threadIdx.x < nR) {
+                    const uint32_t idx = (uint32_t)e[k] >> lg;
+                    tmax = max(tmax, idx);
+                    const uint32_t d = idx - lo;   // wraps for indices below the range
+                    if (d < kDirectMax) {
+                        atomicAdd(&dcnt[d], 1u);
+                        ct_add_sum(&dsum[d], sjbg_fr((uint32_t)(e[k] >> 32)));
+                    }
+                }
+            }
+        }
+        if (p == 0) {
+            const uint32_t m = __reduce_max_sync(0xFFFFFFFFu, tmax);
+            if (lane_id() == 0) atomicMax(&maxidx_s, m);
+        }
+        SJBG_BARRIER();
+        if (p == 0) {
+            passes = maxidx_s / kDirectMax + 1;
+            if (passes > kDirectPasses) {   // too wide: undo the first pass, the hash table takes the bucket
+                for (uint32_t i = threadIdx.x; i < nR; i += blockDim.x) {
+                    const uint32_t d = (uint32_t)Rb[i] >> lg;
+                    if (d < kDirectMax) {
+                        dcnt[d] = 0;
+                        dsum[d] = 0;
+                    }
+                }
+                SJBG_BARRIER();
+                return false;
+            }
+        }
+        // probe: the right keys in the range
+        for (uint32_t base = 0; base < nS; base += tile) {
+            uint64_t e[kJoinPer];
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t j = base + k * blockDim.x + threadIdx.x;
+                e[k] = j < nS ? Sb[j] : 0ull;
+            }
+#pragma unroll
+            for (int k = 0; k < kJoinPer; k++) {
+                const uint32_t d = ((uint32_t)e[k] >> lg) - lo;
+                if (base + k * blockDim.x + threadIdx.x < nS && d < kDirectMax) {
+                    const uint32_t c = dcnt[d];
+                    if (c) {
+                        count += c;
+                        prod += dsum[d] * sjbg_gs((uint32_t)(e[k] >> 32));
+                    }
+                }
+            }
+        }
+        SJBG_BARRIER();
+        // leave the table zero: the range's build entries (the left run again, from L2)
+        for (uint32_t i = threadIdx.x; i < nR; i += blockDim.x) {
+            const uint32_t d = ((uint32_t)Rb[i] >> lg) - lo;
+            if (d < kDirectMax) {
+                dcnt[d] = 0;
+                dsum[d] = 0;
+            }
+        }
+        SJBG_BARRIER();
+    }
+    flush_acc(&acc[bucket_win[b]], count, 0, prod);
+    return true;
+}
+
 constexpr uint32_t kEnumChunk = 4096;  // left tuples per chained chunk
 constexpr uint32_t kNil = 0xFFFFFFFFu;
 
@@ -1129,16 +1252,28 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
 // Bucket joins over the join list (jlist, length *jn; or, without a list,
 // buckets 0 .. B-1): one CTA per item (queue == nullptr) or persistent CTAs
 // that take items from a device work queue (an atomic counter) until it runs dry.
+// With wins (null: hash tables only), the buckets of radix windows are joined
+// through direct tables when their key indices allow it.
 __global__ void __launch_bounds__(kJoinThreads)
 bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
                          const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t cap,
-                         uint32_t *queue, const uint32_t *__restrict__ jlist, const uint32_t *__restrict__ jn) {
+                         uint32_t *queue, const uint32_t *__restrict__ jlist, const uint32_t *__restrict__ jn,
+                         const WinPlan *__restrict__ wins, const LearnedModel *__restrict__ models) {
     const uint32_t items = jlist ? *jn : B;
+    uint32_t clean = 0;
+    auto join = [&](uint32_t b) {
+        if (wins) {
+            const WinPlan &wp = wins[bucket_win[b]];
+            if (!model_of(wp, models) && cnt[b] + cnt[B + b] <= kDirectMaxRun &&
+                join_count_direct(b, partL, partR, start, cnt, B, bucket_win, acc, wp.log2_buckets, clean))
+                return;
+        }
+        join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, cap);
+        clean = 0;
+    };
     if (!queue) {
-        if (blockIdx.x < items)
-            join_count_bucket(jlist ? jlist[blockIdx.x] : blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc,
-                              cap);
+        if (blockIdx.x < items) join(jlist ? jlist[blockIdx.x] : blockIdx.x);
         return;
     }
     __shared__ uint32_t item_s;
@@ -1148,7 +1283,7 @@ bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restric
         SJBG_BARRIER();
         const uint32_t it = item_s;
         if (it >= items) break;
-        join_count_bucket(jlist ? jlist[it] : it, partL, partR, start, cnt, B, bucket_win, acc, cap);
+        join(jlist ? jlist[it] : it);
     }
 }
 
@@ -1402,7 +1537,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
                           (const uint32_t *)dJlist, (const uint32_t *)dJn));
     } else {
         const uint32_t cap = count_table_cap((uint32_t)target);
-        const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
+        const size_t smem =
+            std::max((sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16, kDirectBytes);
         allow_big_smem(bucket_join_count_kernel, smem);
         if (queue) {   // as many persistent CTAs as fit on an SM at this table size (at most 2 by registers)
             const uint32_t per_sm = std::max<uint32_t>(1, (uint32_t)((228u << 10) / (smem + 1024)));
@@ -1410,7 +1546,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         }
         SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, jgrid, dim3(kJoinThreads), smem,
                           dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, cap, queue, (const uint32_t *)dJlist,
-                          (const uint32_t *)dJn));
+                          (const uint32_t *)dJn, (const WinPlan *)dPlan, dModels));
     }
     return SJBG_OK;
 }
@@ -1546,7 +1682,7 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
         bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, rs->acc, cap, nullptr,
-                                                                nullptr, nullptr);
+                                                                nullptr, nullptr, nullptr, nullptr);
         if (int rc = launched("sjbg_lazy_hj_noalloc: bucket_join_count_kernel")) return rc;
     }
     raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);

@@ -198,8 +198,10 @@ def test_learned_keeps_its_model_when_many_keys_are_hot(lib, oracle, z):
 def test_config_skewed_8x2p24_full_size(lib, oracle, z):
     """The skewed workload at its full size: 8 windows of 2^24 tuples per stream,
     keys Zipf(z) over [0, 2^24) with ranks permuted (seed 3), R seed 1, S seed 2.
-    In every window, learned partitioning and radix partitioning at 2^10 both
-    equal the oracle's count and prod."""
+    In every window, learned partitioning, radix partitioning at 2^10, and the
+    learned pipeline with a one-leaf model (light tuples bucketed by one line
+    over their key range, i.e. radix by key range behind the same heavy-key
+    set and compaction) all equal the oracle's count and prod."""
     D, W, nw = 1 << 24, 1 << 24, 8
     table = oracle.zipf_table(D, z)
     left = oracle.gen_zipf(0, nw * W, 1, table, D, 3, threads=16)
@@ -211,8 +213,12 @@ def test_config_skewed_8x2p24_full_size(lib, oracle, z):
     with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_RADIX, radix_bits=10,
                     max_tuples_per_window=W) as j:
         rad = j.lazy_execute_batch(left, right, descs)
-    for i, (g, r, w) in enumerate(zip(got, rad, want)):
-        assert (g["count"], g["prod"]) == (w["count"], w["prod"]) == (r["count"], r["prod"]), i
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, partitioner=lib.PART_LEARNED, learned_leaves=1,
+                    max_tuples_per_window=W) as j:
+        one = j.lazy_execute_batch(left, right, descs)
+    for i, (g, r, o, w) in enumerate(zip(got, rad, one, want)):
+        assert (g["count"], g["prod"]) == (w["count"], w["prod"]) == (r["count"], r["prod"]) == \
+            (o["count"], o["prod"]), i
     if z == 1.5:
         assert all(g["partitioner_used"] == lib.PART_LEARNED for g in got)
 
