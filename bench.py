@@ -718,11 +718,69 @@ def suite_skewed(args, sjbg, torch, dev, z):
     return out
 
 
+def suite_ring(args, sjbg, torch, dev):
+    """Config 1 (16 windows x 65,536 per stream, keys U[0, 65,536)) fed batch by
+    batch (4,096 tuples) from pinned host memory, end to end on the host clock:
+    through the device-resident ingest ring (sjbg_ring_*: batches copied into
+    HBM as they arrive, each window joined there while the next fills) and
+    through the reference's per-window form (sjbg_lazy_execute_ring: the
+    window's batches gathered from a host ring and copied per call)."""
+    W, nw, B, D = 65536, 16, 4096, 65536
+    n = nw * W
+    d = torch.empty(2 * n * 16, dtype=torch.uint8, device="cuda")
+    g = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, device=dev)
+    g.generate(d.data_ptr(), 0, n, 1, D)
+    g.generate(d.data_ptr() + 16 * n, 0, n, 2, D)
+    g.close()
+    h = torch.empty(2 * n * 16, dtype=torch.uint8, pin_memory=True)
+    h.copy_(d)
+    torch.cuda.synchronize()
+    ptr = [h.data_ptr(), h.data_ptr() + 16 * n]
+    j = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, batch_size=B, max_tuples_per_window=W, device=dev)
+
+    def ring_pass():
+        j.ring_open(W, 4)
+        for b in range(n // B):
+            j.ring_push(ptr[0] + 16 * b * B, True, n=B)
+            j.ring_push(ptr[1] + 16 * b * B, False, n=B)
+        st = j.ring_close()
+        return j.ring_poll(64), st
+
+    ring_pass()
+    reps, t0 = 5, time.perf_counter()
+    for _ in range(reps):
+        res, st = ring_pass()
+    ring_s = (time.perf_counter() - t0) / reps
+    tuples = h.numpy().view(sjbg.TUPLE_DTYPE)
+    left, right = tuples[:n], tuples[n:]
+    offs = [[(k * W + i * B) for i in range(W // B)] for k in range(nw)]
+
+    def ref_pass():
+        return [j.lazy_execute_ring(left, offs[k], right, offs[k]) for k in range(nw)]
+
+    ref_pass()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ref = ref_pass()
+    ref_s = (time.perf_counter() - t0) / reps
+    j.close()
+    same = [(r["count"], r["prod"]) for r in res] == [(r["count"], r["prod"]) for r in ref]
+    return {"value": 2 * n / ring_s, "unit": "tuples/s", "wall_ms": ring_s * 1e3,
+            "per_window_calls": {"value": 2 * n / ref_s, "wall_ms": ref_s * 1e3,
+                                 "call": "sjbg_lazy_execute_ring per window (host ring + batch offsets)"},
+            "latency": {"p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                        "unit": "ms from a window's last copy to the end of its join"},
+            "outputs_identical": same, "h2d_bytes_per_step": 32 * n,
+            "workload": "16 windows x 65,536 per stream, keys U[0, 65,536), pinned host batches of 4,096, "
+                        "host wall clock"}
+
+
 def config_suite(args, sjbg, torch, dev, peak, sm_mhz):
     """The other configurations, each under the same run's clock."""
     suite = {}
     t0 = time.perf_counter()
     suite["c1_uniform_hj"] = suite_uniform(args, sjbg, torch, dev, peak)
+    suite["c1_device_ring"] = suite_ring(args, sjbg, torch, dev)
     suite["c3_skewed_z1.0"] = suite_skewed(args, sjbg, torch, dev, 1.0)
     suite["c3_skewed_z0.5"] = suite_skewed(args, sjbg, torch, dev, 0.5)
     suite["c2_eager_smj"] = suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, "SMJ", 1 << 20, 1 << 20, 1024)
@@ -983,6 +1041,27 @@ def main():
     e2e_s = sorted(call_s)[len(call_s) // 2]
     e2e_mean_s = sum(call_s) / len(call_s)
     e2e_same = [(r.count, r.prod_checksum) for r in e2e_res] == [(a[0], a[1]) for a in res_learned]
+    # the same windows pushed in batches of 2^20 tuples through the device-resident
+    # ingest ring: copies of window k+1 overlap the join of window k
+    ring = sjbg.Joiner(partitioner=primary_part, **flags_common)
+    RB = 1 << 20
+
+    def ring_pass():
+        ring.ring_open(W, 3)
+        for a in range(0, total, RB):
+            ring.ring_push(hL.data_ptr() + 16 * a, True, n=min(RB, total - a))
+            ring.ring_push(hR.data_ptr() + 16 * a, False, n=min(RB, total - a))
+        ring.ring_close()
+        return ring.ring_poll(nwin)
+
+    ring_pass()
+    ring_s = []
+    for _ in range(ksteps):
+        t0 = time.perf_counter()
+        ring_res = ring_pass()
+        ring_s.append(time.perf_counter() - t0)
+    ring_same = [(r["count"], r["prod"]) for r in ring_res] == [(a[0], a[1]) for a in res_learned]
+    ring.close()
     # the host link the end-to-end number is bound by: one plain pinned -> device
     # copy of the left stream, event-timed (the step copies both streams)
     link = torch.empty_like(hL, device="cuda")
@@ -1026,7 +1105,10 @@ def main():
         "e2e": {"value": tuples / e2e_s, "mean_value": tuples / e2e_mean_s, "calls": ksteps,
                 "unit": "tuples/s", "h2d_bytes_per_step": 32 * total,
                 "d2h_bytes_per_step": 32 * nwin, "outputs_identical": e2e_same,
-                "h2d_link_gbs": h2d_gbs, "link_bound_tuples_per_s": h2d_gbs * 1e9 / 16},
+                "h2d_link_gbs": h2d_gbs, "link_bound_tuples_per_s": h2d_gbs * 1e9 / 16,
+                "device_ring": {"value": tuples / sorted(ring_s)[len(ring_s) // 2], "unit": "tuples/s",
+                                "outputs_identical": ring_same,
+                                "call": "sjbg_ring_push of pinned batches of 2^20 tuples, sjbg_ring_close"}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,

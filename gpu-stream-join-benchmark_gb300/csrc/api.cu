@@ -20,6 +20,7 @@ sjbg_handle::~sjbg_handle() {
     if (device >= 0) cudaSetDevice(device);
     eager.reset();
     streaming.reset();
+    ring.reset();
     for (auto &g : graphs) {
         if (g->exec) cudaGraphExecDestroy(g->exec);
         for (auto &b : g->pinned)

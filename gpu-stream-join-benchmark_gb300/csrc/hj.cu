@@ -1032,7 +1032,7 @@ constexpr uint32_t kDirectMax = 8192;
 constexpr uint32_t kDirectPasses = 2;
 // Larger buckets (a radix window's hot keys) keep the hash table: every extra
 // pass and the table reset re-read the bucket, which one CTA would do serially.
-constexpr uint32_t kDirectMaxRun = 32768;
+constexpr uint32_t kDirectMaxRun = 16384;
 constexpr size_t kDirectBytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * kDirectMax;
 
 // `clean`: the leading table entries known to be zero (CTA-uniform); a direct

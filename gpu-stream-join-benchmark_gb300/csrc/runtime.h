@@ -37,6 +37,10 @@ struct DevBuf {
 
 struct EagerState;
 struct StreamState;
+struct RingState;   // device-resident ingest ring (ring.cu)
+struct RingDeleter {
+    void operator()(RingState *p) const;
+};
 
 }  // namespace sjbg
 
@@ -85,6 +89,7 @@ struct sjbg_handle {
 
     std::unique_ptr<sjbg::EagerState> eager;
     std::unique_ptr<sjbg::StreamState> streaming;
+    std::unique_ptr<sjbg::RingState, sjbg::RingDeleter> ring;
 
     ~sjbg_handle();
 };

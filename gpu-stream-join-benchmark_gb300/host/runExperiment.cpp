@@ -12,7 +12,9 @@
 // (default 1000), gpuDevice (CUDA device of the joiners and of the power
 // sampler, default 0), usePK ("Yes" / "No", default "No": the reference's
 // EagerJoinConfig::usePK, include/experiment/Config.hpp:15 - eager joiners
-// run as one persistent kernel fed by a queue).  --list prints the expanded configurations and their
+// run as one persistent kernel fed by a queue), deviceRing ("Yes" / "No",
+// default "No": lazy windows over the device-resident ingest ring instead of
+// the pinned host ring; NoOutput only).  --list prints the expanded configurations and their
 // algorithm names without touching a GPU.
 #include <cuda_runtime.h>
 
@@ -301,6 +303,11 @@ int main(int argc, char **argv) {
         if (y.has("sourceThreads")) ec.sourceThreads = std::stoull(y.scalar("sourceThreads"));
         if (y.has("tsUpperBound")) ec.dataConfig.timestampUpperBound = std::stoull(y.scalar("tsUpperBound"));
         if (y.has("gpuDevice")) ec.engineConfig.gpuDevice = std::stoi(y.scalar("gpuDevice"));
+        if (y.has("deviceRing")) {
+            const std::string dr = y.scalar("deviceRing");
+            if (dr != "Yes" && dr != "No") throw std::invalid_argument("Unknown parameter for deviceRing: " + dr);
+            ec.engineConfig.deviceRing = dr == "Yes";
+        }
         if (y.has("usePK")) {
             const std::string pk = y.scalar("usePK");
             if (pk != "Yes" && pk != "No") throw std::invalid_argument("Unknown parameter for usePK: " + pk);

@@ -255,6 +255,60 @@ void CountBased::execute() {
     impl->pool.push(joiner);
 }
 
+// ---- Lazy::DeviceRing ----
+DeviceRing::DeviceRing(Sink &sink, uint64_t windowSize, uint64_t batchSize, uint32_t depth, const sjbg_config &cfg,
+                       std::string name)
+    : BaseWindowing(sink, std::move(name)), h(create_handle(cfg)), windowSize(windowSize), batchSize(batchSize) {
+    const int rc = sjbg_ring_open(h, windowSize, depth);
+    if (rc != SJBG_OK) {
+        std::string msg = sjbg_last_error(h);
+        sjbg_destroy(h);
+        throw std::runtime_error("sjbg_ring_open failed: " + msg);
+    }
+}
+
+DeviceRing::~DeviceRing() { sjbg_destroy(h); }
+
+void DeviceRing::drain() {
+    sjbg_stream_window res[64];
+    uint32_t n = 0;
+    do {
+        const int rc = sjbg_ring_poll(h, res, 64, &n);
+        if (rc != SJBG_OK) throw_sjbg(h, rc, "sjbg_ring_poll");
+        for (uint32_t i = 0; i < n; i++) {
+            const sjbg_window_result &r = res[i].result;
+            if (r.status != SJBG_OK) throw_sjbg(h, (int)r.status, "ring window join");
+            sink.addChecksums(r.xor_checksum, r.prod_checksum);
+            sink.addToPossibleMatches(res[i].n_left * res[i].n_right);
+            sink.addToCounter(r.count, true);
+            ExecutionStatistic st;
+            st.resultCount = r.count;
+            st.probeTime = (uint64_t)(r.ms * 1000.0f);   // device time of the window's join, microseconds
+            sink.addToStatistics(st);
+            sink.addToExecutedWindows(1);
+        }
+    } while (n == 64);
+}
+
+void DeviceRing::push(Tuple *batch, bool left) {
+    std::lock_guard<std::mutex> g(mu);
+    const int rc = sjbg_ring_push(h, reinterpret_cast<const sjbg_tuple *>(batch), batchSize, left ? 1 : 0,
+                                  SJBG_MEM_HOST);
+    // the reference exits the process here ("Ring buffer is full")
+    if (rc == SJBG_E_CAPACITY) throw std::runtime_error("Ring buffer is full");
+    if (rc != SJBG_OK) throw_sjbg(h, rc, "sjbg_ring_push");
+    drain();
+}
+
+void DeviceRing::onEndOfStream() {
+    std::lock_guard<std::mutex> g(mu);
+    if (closed) return;
+    closed = true;
+    const int rc = sjbg_ring_close(h, nullptr);
+    if (rc != SJBG_OK) throw_sjbg(h, rc, "sjbg_ring_close");
+    drain();
+}
+
 }  // namespace Lazy
 
 // ---- Eager::CountBased (include/sjb/windowing/eager/CountBased.cuh:36-72) ----
@@ -365,6 +419,15 @@ std::shared_ptr<BaseWindowing> WindowingFactory::create(AlgorithmConfig algorith
                                                         Sink &sink) {
     const std::string name = algorithmName(algorithmConfig);
     const sjbg_config cfg = toConfig(algorithmConfig, dataConfig, queryConfig, engineConfig);
+    if (algorithmConfig.progressiveness == PROGRESSIVENESS_TYPE::LAZY && engineConfig.deviceRing) {
+        // the ring's joins report counts and checksums, no pairs
+        if (algorithmConfig.resultWritingMethod != RESULT_WRITING_METHOD::NoOutput)
+            throw std::runtime_error("Not Implemented");
+        const uint64_t slots = queryConfig.windowSize ? engineConfig.ringBufferSize / queryConfig.windowSize : 0;
+        const uint32_t depth = (uint32_t)std::min<uint64_t>(64, std::max<uint64_t>(2, slots));
+        return std::make_shared<Lazy::DeviceRing>(sink, queryConfig.windowSize, dataConfig.batchSize, depth, cfg,
+                                                  name + "_ring");
+    }
     if (algorithmConfig.progressiveness == PROGRESSIVENESS_TYPE::LAZY) {
         std::vector<std::shared_ptr<Lazy::Executor::BaseLazyExecutor>> joiners;
         const uint64_t n = std::max<uint64_t>(1, std::min(engineConfig.joinerThreads, kMaxGpuJoiners));

@@ -133,6 +133,7 @@ struct EngineConfig {
     uint64_t nSourceThreads;
     uint64_t maxTupleInWindow;
     int gpuDevice = 0;   // CUDA device of the GPU joiners (no reference counterpart)
+    bool deviceRing = false;   // lazy windows over the device-resident ring (no reference counterpart)
 };
 
 namespace Windowing {
@@ -227,6 +228,29 @@ private:
     Tuple *ring[2] = {nullptr, nullptr};   // pinned host memory (cudaMallocHost), as the reference's
     bool ringPinned = false;               // false: no CUDA device, plain host memory
     std::deque<uint64_t> available[2], executable[2];
+    std::mutex mu;
+};
+// Count-based tumbling windows over a device-resident ring (sjbg_ring_*, the
+// optional YAML key deviceRing: "Yes"): each batch is copied into HBM as it
+// arrives, and each full window is joined there, asynchronously, while the
+// next one fills.  Results reach the sink as the joins finish.  The windows
+// are those of CountBased above (tuples [kW, (k+1)W) of each side in arrival
+// order); its pinned host ring and per-window copies are what this replaces.
+class DeviceRing : public BaseWindowing {
+public:
+    DeviceRing(Sink &sink, uint64_t windowSize, uint64_t batchSize, uint32_t depth, const sjbg_config &cfg,
+               std::string name);
+    ~DeviceRing() override;
+    void onIncomingLeft(Tuple *tupleBuffer) override { push(tupleBuffer, true); }
+    void onIncomingRight(Tuple *tupleBuffer) override { push(tupleBuffer, false); }
+    void onEndOfStream() override;
+
+private:
+    void push(Tuple *batch, bool left);
+    void drain();   // finished windows into the sink (caller holds mu)
+    sjbg_handle *h = nullptr;
+    uint64_t windowSize, batchSize;
+    bool closed = false;
     std::mutex mu;
 };
 }  // namespace Lazy

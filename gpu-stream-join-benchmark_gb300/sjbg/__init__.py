@@ -40,6 +40,7 @@ EXPORTS = [
     "sjbg_eager_execute", "sjbg_eager_clear_states", "sjbg_eager_window_result", "sjbg_eager_end_of_stream",
     "sjbg_eager_post", "sjbg_eager_wait", "sjbg_eager_pk_status",
     "sjbg_eager_run", "sjbg_stream_open", "sjbg_stream_push", "sjbg_stream_poll", "sjbg_stream_close",
+    "sjbg_ring_open", "sjbg_ring_push", "sjbg_ring_poll", "sjbg_ring_close",
     "sjbg_generate", "sjbg_kernel_stats", "sjbg_kernel_stats_reset", "sjbg_launch_count",
     "sjbg_lazy_hj_noalloc", "sjbg_zipf_table",
 ]
@@ -137,6 +138,10 @@ def load(path: str = LIB_PATH):
         L.sjbg_stream_push.argtypes = [vp, vp, u64, i32, u32]
         L.sjbg_stream_poll.argtypes = [vp, vp, u32, C.POINTER(u32)]
         L.sjbg_stream_close.argtypes = [vp, C.POINTER(StreamStats)]
+        L.sjbg_ring_open.argtypes = [vp, u64, u32]
+        L.sjbg_ring_push.argtypes = [vp, vp, u64, i32, u32]
+        L.sjbg_ring_poll.argtypes = [vp, vp, u32, C.POINTER(u32)]
+        L.sjbg_ring_close.argtypes = [vp, C.POINTER(StreamStats)]
         L.sjbg_generate.argtypes = [vp, vp, u64, u64, u64, u64, vp, u64]
         L.sjbg_kernel_stats.argtypes = [vp, u32, C.c_char_p, C.c_size_t, C.POINTER(u64), C.POINTER(C.c_double)]
         L.sjbg_kernel_stats_reset.argtypes = [vp]
@@ -331,6 +336,26 @@ class Joiner:
     def stream_close(self):
         st = StreamStats()
         self._check(self.lib.sjbg_stream_close(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in StreamStats._fields_}
+
+    # ---- device-resident ingest ring (count-based lazy windows)
+    def ring_open(self, window_tuples: int, depth: int = 4):
+        self._check(self.lib.sjbg_ring_open(self.h, window_tuples, depth))
+
+    def ring_push(self, batch, is_left: bool, mem=MEM_HOST, n=None):
+        self._check(self.lib.sjbg_ring_push(self.h, _ptr(batch), n if n is not None else _len(batch),
+                                            int(is_left), mem))
+
+    def ring_poll(self, max_out=1024):
+        """Finished windows in window order: result fields plus window_id, n_left, n_right."""
+        res = (StreamWindow * max_out)()
+        n = C.c_uint32()
+        self._check(self.lib.sjbg_ring_poll(self.h, C.cast(res, C.c_void_p), max_out, C.byref(n)))
+        return [res[i].as_dict() for i in range(n.value)]
+
+    def ring_close(self):
+        st = StreamStats()
+        self._check(self.lib.sjbg_ring_close(self.h, C.byref(st)))
         return {k: getattr(st, k) for k, _ in StreamStats._fields_}
 
     # ---- utilities

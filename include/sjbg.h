@@ -310,6 +310,31 @@ SJBG_API int sjbg_stream_push(sjbg_handle *h, const sjbg_tuple *batch, uint64_t 
 SJBG_API int sjbg_stream_poll(sjbg_handle *h, sjbg_stream_window *out, uint32_t max_out, uint32_t *n_out);
 SJBG_API int sjbg_stream_close(sjbg_handle *h, sjbg_stream_stats *stats);
 
+/* ---- device-resident ingest ring (count-based lazy windows) ----------------------
+ * Replaces the pinned host ring of Windowing::Lazy::CountBased
+ * (include/sjb/windowing/lazy/CountBased.cuh:45-101: incoming batches are
+ * memmoved into a pinned ring, and a joiner copies each full window to the
+ * device per call).  The ring lives in HBM: `depth` slots of window_tuples
+ * tuples per side; tuples [kW, (k+1)W) of each side in arrival order form
+ * window k (the reference's tumbling count window).  sjbg_ring_push copies a
+ * batch straight into its slot on a copy stream (split where it crosses a
+ * window boundary); once both sides have filled window k its join (the
+ * handle's lazy algorithm, count and checksums, no pairs) is enqueued behind
+ * those copies only, so ingest of window k + 1 overlaps the join of window k.
+ * A pinned host batch is read asynchronously: keep it unchanged until
+ * sjbg_ring_poll has reported every window it contributes to, or
+ * sjbg_ring_close has returned.  A side that gets `depth` windows ahead of the
+ * other makes the push fail with SJBG_E_CAPACITY ("Ring buffer is full", where
+ * the reference exits).  Partial windows at close are not joined, as in the
+ * reference. */
+SJBG_API int sjbg_ring_open(sjbg_handle *h, uint64_t window_tuples, uint32_t depth);
+SJBG_API int sjbg_ring_push(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int is_left, uint32_t mem);
+/* Finished windows in window order (window_id = k; ms = device time from the
+ * window's last copy to the end of its join). */
+SJBG_API int sjbg_ring_poll(sjbg_handle *h, sjbg_stream_window *out, uint32_t max_out, uint32_t *n_out);
+/* Wait for every enqueued join; stats: windows joined, tuples, p50/p99 of ms. */
+SJBG_API int sjbg_ring_close(sjbg_handle *h, sjbg_stream_stats *stats);
+
 /* ---- synthetic inputs on the device ---------------------------------------------
  * Fill n tuples of a stream (global indices first..first+n-1) in device memory:
  * key uniform in [0, domain) when zipf_table is NULL, else Zipf rank from the

@@ -69,6 +69,22 @@ def test_lazy_harness_matches_oracle(harness, oracle, tmp_path, alg, result):
     assert progress == cum
 
 
+@pytest.mark.parametrize("alg", ["HJ", "SMJ"])
+def test_lazy_harness_device_ring_matches_oracle(harness, oracle, tmp_path, alg):
+    """deviceRing: "Yes" replaces the pinned host ring with the device-resident
+    ring: batches land in HBM as they arrive and each window is joined there.
+    Same windows, counts, checksum and per-window progress as the oracle."""
+    left, right = streams(oracle)
+    count, prod, windows, progress = run(harness, tmp_path, alg, "LAZY", extra='deviceRing: "Yes"\n')
+    want = [oracle.join(left[k * W:(k + 1) * W], right[k * W:(k + 1) * W], enumerate_pairs=False)
+            for k in range(N // W)]
+    assert windows == N // W
+    assert count == sum(r["count"] for r in want)
+    assert prod == sum(r["prod"] for r in want) % (1 << 64)
+    assert progress == np.cumsum([r["count"] for r in want]).tolist()
+    assert "lazy_gpu_" + alg.lower() + "_nm_ring" in run.last.stdout
+
+
 def test_lazy_harness_zipf(harness, oracle, tmp_path):
     left, right = streams(oracle, theta=0.9, distinct=1 << 16)
     count, prod, _, _ = run(harness, tmp_path, "HJ", "LAZY", theta="0.9", distinct=1 << 16)

@@ -105,6 +105,13 @@ def test_usage_message(harness):
     assert r.returncode == 1 and "runExperiment <path_to_yaml_config> <outputFileName>" in r.stdout
 
 
+def test_device_ring_key(harness, tmp_path):
+    rc, _, err = listing(harness, write_yaml(tmp_path, deviceRing='"Maybe"'))
+    assert rc == 2 and "Unknown parameter for deviceRing: Maybe" in err
+    rc, rows, _ = listing(harness, write_yaml(tmp_path, deviceRing='"Yes"'))
+    assert rc == 0 and rows
+
+
 def test_use_pk_key(harness, tmp_path):
     rc, rows, _ = listing(harness, write_yaml(tmp_path, usePK='"Yes"', progressivenessModes='[ "EAGER" ]'))
     assert rc == 0 and rows[0].split(",")[0] == "eager_gpu_hj_pk_nm"
