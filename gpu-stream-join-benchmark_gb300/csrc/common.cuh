@@ -102,6 +102,17 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, uint32_t *total) 
     return x - v;
 }
 
+// Prefetch the 16-byte aligned part of [p, p + bytes) into L2 with one bulk
+// request (at most 256 KiB; nothing outside the range is touched, no completion
+// to wait for).
+__device__ __forceinline__ void l2_prefetch_bulk(const void *p, size_t bytes) {
+    const uintptr_t a = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+    uintptr_t e = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+    if (e > a + (256u << 10)) e = a + (256u << 10);
+    if (e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)) : "memory");
+}
+
 // Global nanosecond timer for bounded waits.
 __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;

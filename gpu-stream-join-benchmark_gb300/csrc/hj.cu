@@ -600,27 +600,71 @@ __device__ void block_scan_smem(uint32_t *a, uint32_t P, uint32_t *warp_tot) {
 }
 
 // ------------------------------------------------------------------ 3. scatter
-__device__ __forceinline__ void scatter_tile(const WorkItem it, const sjbg_tuple *__restrict__ L,
+constexpr int kScatterPer = kTile / kPartThreads;   // tuples per thread per tile
+
+// Where a scatter work item's tuples are: the window side's tuples, or (a
+// compacted window) the light tuples the counting pass packed as 8-byte words.
+struct TileIn {
+    const void *p;
+    uint32_t n;        // tuples in the tile
+    uint32_t packed;   // 8-byte (key, val) words rather than 16-byte tuples
+};
+
+__device__ __forceinline__ TileIn tile_input(const WorkItem it, const sjbg_tuple *__restrict__ L,
                                              const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                                              const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
-                                             uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL,
-                                             uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
+                                             const LearnedModel *__restrict__ models,
                                              const uint64_t *__restrict__ compL, const uint64_t *__restrict__ compR,
                                              const uint32_t *__restrict__ ccnt) {
-    extern __shared__ __align__(16) uint8_t smem_raw[];
-    __shared__ uint32_t warp_tot[32];
     const bool right = it.right;
     const uint32_t w = it.w;
-    const uint32_t *tp = right ? tileR : tileL;
-    const WinPlan wp = wins[w];
+    const WinPlan &wp = wins[w];
     const LearnedModel *gm = model_of(wp, models);
-    // compacted windows: the tiles cover the light tuples the counting pass wrote out
     const bool compact = gm && gm->n_heavy && gm->compact;
     const uint64_t nside = compact ? ccnt[2 * w + (right ? 1 : 0)] : (right ? wp.n_right : wp.n_left);
     const uint64_t start = (uint64_t)it.local * kTile;
-    const uint32_t n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
-    const uint4 *src = reinterpret_cast<const uint4 *>((right ? R + wp.right_off : L + wp.left_off) + start);
-    const uint64_t *csrc = compact ? (right ? compR : compL) + (uint64_t)tp[w] * kTile + start : nullptr;
+    TileIn t;
+    t.n = (uint32_t)(nside - start < (uint64_t)kTile ? nside - start : (uint64_t)kTile);
+    t.packed = compact ? 1u : 0u;
+    if (compact)
+        t.p = (right ? compR : compL) + (uint64_t)(right ? tileR : tileL)[w] * kTile + start;
+    else
+        t.p = (right ? R + wp.right_off : L + wp.left_off) + start;
+    return t;
+}
+
+// The thread's tuples of a tile as (val << 32 | key) words, every load in flight before any use.
+__device__ __forceinline__ void tile_load(const TileIn &t, uint64_t (&e)[kScatterPer]) {
+#pragma unroll
+    for (int k = 0; k < kScatterPer; k++) {
+        const uint32_t i = threadIdx.x + k * kPartThreads;
+        if (i < t.n) {
+            if (t.packed) {
+                e[k] = __ldg(static_cast<const uint64_t *>(t.p) + i);
+            } else {
+                const uint2 v = __ldg(reinterpret_cast<const uint2 *>(static_cast<const sjbg_tuple *>(t.p) + i));
+                e[k] = ((uint64_t)v.y << 32) | v.x;   // key and val only
+            }
+        }
+    }
+}
+
+// One tile whose tuples are already in e[]: local counting sort by bucket in
+// shared memory, one global reservation per non-empty bucket, contiguous
+// per-bucket runs written out.  As soon as the tile is staged in shared memory
+// e[] is free, so the next tile's loads (next, when given) are issued into it
+// before this tile's write-out: they are in flight while it runs.
+__device__ __forceinline__ void scatter_tile(const WorkItem it, const TileIn in, uint64_t (&e)[kScatterPer],
+                                             const TileIn *next, const WinPlan *__restrict__ wins,
+                                             uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL,
+                                             uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ uint32_t warp_tot[32];
+    const bool right = it.right;
+    const WinPlan wp = wins[it.w];
+    const LearnedModel *gm = model_of(wp, models);
+    const bool compact = in.packed != 0;
+    const uint32_t n = in.n;
     // a model buckets into its own (often smaller) fan-out: only those counters are touched
     const uint32_t P = 1u << (gm ? gm->log2_buckets : wp.log2_buckets);
 
@@ -638,23 +682,9 @@ __device__ __forceinline__ void scatter_tile(const WorkItem it, const sjbg_tuple
     if (threadIdx.x == 0) kept_s = 0;
     if (heavy) heavy_set_load(hs, gm);
     SJBG_BARRIER();
-    constexpr int kPer = kTile / kPartThreads;
-    uint64_t e[kPer];
-    uint32_t bk[kPer], rk[kPer];
+    uint32_t bk[kScatterPer], rk[kScatterPer];
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {   // all of the thread's loads in flight before any use
-        const uint32_t i = threadIdx.x + k * kPartThreads;
-        if (i < n) {
-            if (compact) {
-                e[k] = __ldg(csrc + i);
-            } else {
-                const uint2 v = __ldg(reinterpret_cast<const uint2 *>(src + i));   // key and val only
-                e[k] = ((uint64_t)v.y << 32) | v.x;
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
+    for (int k = 0; k < kScatterPer; k++) {
         const uint32_t i = threadIdx.x + k * kPartThreads;
         bk[k] = kHeavyBucket;
         if (i < n) {
@@ -666,6 +696,9 @@ __device__ __forceinline__ void scatter_tile(const WorkItem it, const sjbg_tuple
         }
     }
     SJBG_BARRIER();
+    // the next tile into L2 (its address is known by now), so that the register
+    // loads issued once this tile is staged find it there
+    if (next && threadIdx.x == 0) l2_prefetch_bulk(next->p, (size_t)next->n * (next->packed ? 8u : 16u));
     // reserve one global range per non-empty bucket
     uint32_t *gcur = cursor + (right ? B : 0) + wp.bucket_base;
     uint32_t kept = 0;
@@ -678,13 +711,14 @@ __device__ __forceinline__ void scatter_tile(const WorkItem it, const sjbg_tuple
     block_scan_smem(lcnt, P, warp_tot);   // lcnt -> local offsets (ends with a barrier)
     const uint32_t nk = heavy ? kept_s : n;
 #pragma unroll
-    for (int k = 0; k < kPer; k++) {
+    for (int k = 0; k < kScatterPer; k++) {
         if (bk[k] != kHeavyBucket) {
             const uint32_t pos = lcnt[bk[k]] + rk[k];
             stage[pos] = e[k];
             sb[pos] = (uint16_t)bk[k];
         }
     }
+    if (next) tile_load(*next, e);
     SJBG_BARRIER();
     uint64_t *out = right ? outR : outL;
     for (uint32_t j = threadIdx.x; j < nk; j += blockDim.x) {
@@ -701,12 +735,27 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
                     const LearnedModel *__restrict__ models, const uint64_t *__restrict__ compL,
                     const uint64_t *__restrict__ compR, const uint32_t *__restrict__ ccnt) {
     // persistent CTAs over the tiles listed by the work prefixes workL / workR
-    // (a compacted window's light tiles; a single-level window's tiles)
+    // (a compacted window's light tiles; a single-level window's tiles), each
+    // tile's loads issued while the previous tile is written out
     const uint32_t items = workL[nwin] + workR[nwin];
-    for (uint32_t bt = blockIdx.x; bt < items; bt += gridDim.x) {
+    uint32_t bt = blockIdx.x;
+    if (bt >= items) return;
+    WorkItem it = work_item(workL, workR, nwin, bt);
+    TileIn in = tile_input(it, L, R, wins, tileL, tileR, models, compL, compR, ccnt);
+    uint64_t e[kScatterPer];
+    tile_load(in, e);
+    for (; bt < items; bt += gridDim.x) {
         SJBG_BARRIER();   // the previous tile's shared-memory readers are done
-        scatter_tile(work_item(workL, workR, nwin, bt), L, R, wins, tileL, tileR, cursor, B, outL, outR, models,
-                     compL, compR, ccnt);
+        const uint32_t nb = bt + gridDim.x;
+        WorkItem nit = it;
+        TileIn nin = in;
+        if (nb < items) {
+            nit = work_item(workL, workR, nwin, nb);
+            nin = tile_input(nit, L, R, wins, tileL, tileR, models, compL, compR, ccnt);
+        }
+        scatter_tile(it, in, e, nb < items ? &nin : nullptr, wins, cursor, B, outL, outR, models);
+        it = nit;
+        in = nin;
     }
 }
 
