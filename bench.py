@@ -283,6 +283,32 @@ def bench_batched(args, sjbg, torch, dev):
                   "notes": "hash join autotuned + CUDA-graph replay; sort-merge graph replay (radix passes whose digit is zero in every key skip themselves on the device)"})
 
 
+def bench_batched_small(args, sjbg, torch, dev, nw=160):
+    """A reduced case of the batched workload for profiler captures: its first
+    160 windows (about 25 M tuples per stream, inputs larger than L2), radix
+    partitioning, un-graphed calls on the handle's stream."""
+    sizes = [sjbg_log_uniform(w) for w in range(nw)]
+    total = sum(sizes)
+    dl = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    dr = torch.empty(total * 16, dtype=torch.uint8, device="cuda")
+    j = sjbg.Joiner(sjbg.ALG_HJ, sjbg.LAZY, partitioner=sjbg.PART_RADIX, max_tuples_per_window=1 << 20, device=dev)
+    descs_l, off = [], 0
+    for n in sizes:
+        j.generate(dl.data_ptr() + 16 * off, off, n, 1, 4 * n)
+        j.generate(dr.data_ptr() + 16 * off, off, n, 2, 4 * n)
+        descs_l.append((off, n, off, n, 0, 0))
+        off += n
+    descs = (sjbg.WindowDesc * nw)(*[sjbg.WindowDesc(*d) for d in descs_l])
+    res = (sjbg.WindowResult * nw)()
+    stream = torch.cuda.Stream()
+    j.set_stream(stream.cuda_stream)
+    ms = _events_time(torch, stream, lambda: j.lazy_execute_batch_raw(dl.data_ptr(), dr.data_ptr(), descs, res),
+                      max(1, args.steps), args.warmup)
+    j.close()
+    return _line("joined input tuples/s", 2 * total / (ms * 1e-3), "tuples/s", ms, args, "batched_small_radix",
+                 {"windows": nw, "tuples_per_step": 2 * total, "matches": sum(r.count for r in res)})
+
+
 def sjbg_log_uniform(w, lo=1 << 10, hi=1 << 20, seed=4):
     """Window length w of the batched workload (the generator's log-uniform draw)."""
     import math
@@ -803,6 +829,7 @@ def config_suite(args, sjbg, torch, dev, peak, sm_mhz):
 
 SPECIAL = {
     "batched_1024": bench_batched,
+    "batched_small_radix": bench_batched_small,
     "eager_smj_2p20": bench_eager_smj,
     "eager_nlj_65536": bench_eager_nlj,
     "stream_0.5g": lambda a, s, t, d: bench_stream(a, s, t, d, rate=0.5e9),
