@@ -48,6 +48,8 @@ WORKLOADS = {
     "skewed_hj_small_z1.0": (2, 1 << 22, 1 << 24, 1.0),
     # two windows large enough for two-level partitioning (2^11 buckets)
     "skewed_hj_mid_z1.0": (2, 1 << 23, 1 << 24, 1.0),
+    # two windows of the headline's size (its per-window sample and model work) for captures
+    "skewed_hj_2x2p24": (2, 1 << 24, 1 << 24, 1.5),
 }
 
 
@@ -1099,6 +1101,22 @@ def main():
     ev1.record()
     torch.cuda.synchronize()
     h2d_gbs = hL.numel() / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
+    # the same bytes as two halves copied at once on two streams (two copy engines)
+    half = hL.numel() // 2
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    ev2 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record()
+    s1.wait_event(ev0)
+    s2.wait_event(ev0)
+    with torch.cuda.stream(s1):
+        link[:half].copy_(hL[:half], non_blocking=True)
+    with torch.cuda.stream(s2):
+        link[half:].copy_(hL[half:], non_blocking=True)
+    ev1.record(s1)
+    ev2.record(s2)
+    torch.cuda.synchronize()
+    h2d_gbs_two = hL.numel() / (max(ev0.elapsed_time(ev1), ev0.elapsed_time(ev2)) * 1e-3) / 1e9
     del link
 
     tuples = 2 * total * world
@@ -1132,7 +1150,8 @@ def main():
         "e2e": {"value": tuples / e2e_s, "mean_value": tuples / e2e_mean_s, "calls": ksteps,
                 "unit": "tuples/s", "h2d_bytes_per_step": 32 * total,
                 "d2h_bytes_per_step": 32 * nwin, "outputs_identical": e2e_same,
-                "h2d_link_gbs": h2d_gbs, "link_bound_tuples_per_s": h2d_gbs * 1e9 / 16,
+                "h2d_link_gbs": h2d_gbs, "h2d_link_gbs_two_streams": h2d_gbs_two,
+                "link_bound_tuples_per_s": max(h2d_gbs, h2d_gbs_two) * 1e9 / 16,
                 "device_ring": {"value": tuples / sorted(ring_s)[len(ring_s) // 2], "unit": "tuples/s",
                                 "outputs_identical": ring_same,
                                 "call": "sjbg_ring_push of pinned batches of 2^20 tuples, sjbg_ring_close"}},

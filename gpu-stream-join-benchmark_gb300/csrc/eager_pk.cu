@@ -243,7 +243,7 @@ __device__ int pk_follow(const PkArgs &a, unsigned long long t, PkWork *w) {
             atomicOr(&s->err, kErrTimeout);
             return 1;
         }
-        __nanosleep(128);
+        __nanosleep(32);
     }
     __threadfence();
     const volatile PkWork *v = &s->work;
@@ -633,6 +633,7 @@ struct PkState {
     int grid = 0;
     size_t smem = 0;
     bool running = false;
+    bool host_direct = false;   // the GPU reads pageable host memory coherently (address translation services)
     bool broken = false;        // a ticket failed on the device: batches refused until the window is cleared
     bool reset_state = true;    // clear the device window state before the next launch
     uint64_t launches = 0;
@@ -724,10 +725,17 @@ static int pk_init(sjbg_handle *h) {
         cudaGetLastError();
         return fail(h, SJBG_E_UNSUPPORTED, "persistent eager kernel does not fit an SM");
     }
-    // HJ: enough CTAs for one tuple per thread of a 4,096-tuple batch, the rest of the GPU stays free;
-    // NLJ and SMJ: the whole GPU (their tickets are compare- or bandwidth-heavy)
-    pk->grid = h->cfg.algorithm == SJBG_ALG_HJ ? std::min(32, h->num_sms)
+    // HJ: one tuple per thread of a 4,096-tuple batch (fewer CTAs, fewer arrivals per
+    // ticket), the rest of the GPU stays free; NLJ and SMJ: the whole GPU (their
+    // tickets are compare- or bandwidth-heavy)
+    pk->grid = h->cfg.algorithm == SJBG_ALG_HJ ? std::min(16, h->num_sms)
                                                : std::min(occ, 2) * h->num_sms;
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    pk->host_direct = pageable != 0;
     pk->count.assign(pk->Q, 0);
     pk->status.assign(pk->Q, 0);
     pk->snap.assign(pk->Q, WinAcc{0, 0, 0, 0, 0});
@@ -899,7 +907,13 @@ static int pk_wait(sjbg_handle *h, uint64_t t, unsigned long long *count, WinAcc
 // ---- entry points used by eager.cu on SJBG_F_PERSISTENT handles
 int pk_execute(sjbg_handle *h, const sjbg_tuple *batch, uint64_t n, int side, bool from_host, uint64_t *match) {
     const sjbg_tuple *src = nullptr;
+    if (!h->eager->pk)
+        if (int rc = pk_init(h)) return rc;
     if (!from_host) {
+        src = batch;
+    } else if (h->eager->pk->host_direct) {
+        // the device reads host memory coherently through the host's page tables:
+        // the kernel takes the caller's batch in place (the call waits for the result)
         src = batch;
     } else {
         // pinned caller memory is read by the kernel in place (the call waits for the result)

@@ -54,6 +54,7 @@ struct SampleWin {
     uint64_t list_off;     // first entry of this window's list of keys at or above thresh
     uint32_t list_cap;     // m / thresh + 1: every listed key has at least thresh samples
     uint32_t pad;
+    uint64_t stride[2];    // tuples between run starts, left and right side: n / (runs per side)
 };
 
 struct SampleScratch {
@@ -68,20 +69,28 @@ struct SampleScratch {
 // Sample i of a window: the samples come in runs of 2^run_log2 consecutive
 // tuples (one 128-byte line for runs of 8), even runs from the left side, odd
 // from the right; the j-th run of a side lies in the j-th of its equal strides,
-// at a hashed offset inside it (the high half of hash * room: no division).
+// at a hashed offset inside it (the high half of hash * room: no division),
+// moved to the nearest line start.
 __device__ __forceinline__ uint32_t sample_key(const SampleWin &s, const sjbg_tuple *L, const sjbg_tuple *R, uint32_t i) {
     const uint32_t run = 1u << s.run_log2;
     const uint32_t r = i >> s.run_log2, q = i & (run - 1u);
     const bool right = r & 1u;
     const uint64_t n = right ? s.n_right : s.n_left;
-    const uint64_t runs = s.m >> (s.run_log2 + 1);   // runs per side
     const uint64_t j = r >> 1;
-    const uint64_t stride = n / runs;   // >= run by construction of m, < 2^32 for n < 2^36
+    const uint64_t stride = right ? s.stride[1] : s.stride[0];   // >= run by construction of m, < 2^32 for n < 2^36
     const uint64_t room = stride - run + 1;
     const uint64_t jit = ((uint64_t)(uint32_t)sjbg_mix64(0x5A17ull + r) * (room & 0xFFFFFFFFull)) >> 32;
-    uint64_t idx = j * stride + jit + q;
+    const sjbg_tuple *side = right ? R + s.right_off : L + s.left_off;
+    uint64_t idx = j * stride + jit;
+    if (run == 8) {
+        // a run of 8 tuples starts on a 128-byte line: one line per run, not two.
+        // Rounded down, or up when down would leave the run's stride.
+        const uint64_t a = ((uintptr_t)(side + idx) >> 4) & 7u;
+        idx = idx - a >= j * stride && idx >= a ? idx - a : idx + ((8u - a) & 7u);
+    }
+    idx += q;
     if (idx >= n) idx = n - 1;
-    return right ? R[s.right_off + idx].key : L[s.left_off + idx].key;
+    return side[idx].key;
 }
 
 // Gathers each window's sample into the packed key array (four independent
@@ -111,13 +120,23 @@ sample_minmax_kernel(const sjbg_tuple *L, const sjbg_tuple *R, const SampleWin *
             }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        lo = min(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+    // one pair of global atomics per CTA (every CTA of a window updates the same two words)
+    __shared__ uint32_t lo_s, hi_s;
+    if (threadIdx.x == 0) {
+        lo_s = 0xFFFFFFFFu;
+        hi_s = 0;
     }
+    lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+    hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+    SJBG_BARRIER();
     if (lane_id() == 0) {
-        atomicMin(&scr[w].kmin, lo);
-        atomicMax(&scr[w].kmax, hi);
+        atomicMin(&lo_s, lo);
+        atomicMax(&hi_s, hi);
+    }
+    SJBG_BARRIER();
+    if (threadIdx.x == 0) {
+        atomicMin(&scr[w].kmin, lo_s);
+        atomicMax(&scr[w].kmax, hi_s);
     }
 }
 
@@ -144,6 +163,8 @@ constexpr uint32_t kCountChunk = 2048;
 constexpr uint32_t kCountSlotsLog2 = 12;   // 2 * kCountChunk slots: a free slot always exists
 constexpr uint32_t kCountSlots = 1u << kCountSlotsLog2;
 constexpr uint32_t kNoKey = 0xFFFFFFFFu;   // empty shared slot (the key itself counts in slot kCountSlots)
+constexpr uint32_t kCountPer = kCountChunk / kSampleThreads;   // keys per thread and chunk
+static_assert(kCountChunk % kSampleThreads == 0 && kCountSlots + 1 <= 0xFFFFu, "chunk layout");
 
 __device__ __forceinline__ void count_update(const SampleWin &s, SampleScratch &sc, uint32_t *hw,
                                              unsigned long long *tw, uint32_t *lw, float kmin, float inv, uint32_t k,
@@ -152,17 +173,16 @@ __device__ __forceinline__ void count_update(const SampleWin &s, SampleScratch &
     atomicAdd(&hw[bin_of(key_x(k, kmin, inv))], c);
     uint32_t slot = slot_hash(k, s.table_log2);
     uint32_t before = 0xFFFFFFFFu;   // the key's count before this update
+    // the compare-and-swap claims an empty slot or returns the slot's key (a
+    // count is at least 1, so a taken slot is never 0): one round trip for a
+    // key new to the table, two for a key already in it
     for (uint32_t p = 0; p <= mask; p++) {
-        unsigned long long cur = tw[slot];
-        if (cur == 0ull) {
-            unsigned long long prev = atomicCAS(&tw[slot], 0ull, ((unsigned long long)k << 32) | c);
-            if (prev == 0ull) {
-                before = 0;
-                break;
-            }
-            cur = prev;
+        const unsigned long long prev = atomicCAS(&tw[slot], 0ull, ((unsigned long long)k << 32) | c);
+        if (prev == 0ull) {
+            before = 0;
+            break;
         }
-        if ((uint32_t)(cur >> 32) == k) {
+        if ((uint32_t)(prev >> 32) == k) {
             before = (uint32_t)atomicAdd(&tw[slot], (unsigned long long)c);
             break;
         }
@@ -188,6 +208,8 @@ __global__ void __launch_bounds__(kSampleThreads)
 sample_count_kernel(const uint32_t *keys, const SampleWin *wins, SampleScratch *scr, uint32_t *hist,
                     unsigned long long *table, uint32_t *lists) {
     __shared__ uint32_t skey[kCountSlots], scnt[kCountSlots + 1];
+    __shared__ uint16_t used[kCountChunk + 1];   // slots taken by the chunk's distinct keys
+    __shared__ uint32_t n_used;
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
     float kmin, inv;
@@ -201,33 +223,53 @@ sample_count_kernel(const uint32_t *keys, const SampleWin *wins, SampleScratch *
         if (j < kCountSlots) skey[j] = kNoKey;
         scnt[j] = 0;
     }
+    if (threadIdx.x == 0) n_used = 0;
     SJBG_BARRIER();
     for (uint32_t base = blockIdx.x * kCountChunk; base < s.m; base += gridDim.x * kCountChunk) {
         const uint32_t end = min(base + kCountChunk, s.m);
-        for (uint32_t i = base + threadIdx.x; i < end; i += blockDim.x) {
-            const uint32_t k = kw[i];
-            if (k == kNoKey) {
-                atomicAdd(&scnt[kCountSlots], 1u);
-                continue;
-            }
-            uint32_t slot = slot_hash(k, kCountSlotsLog2);
-            for (uint32_t p = 0; p < kCountSlots; p++) {
-                const uint32_t prev = atomicCAS(&skey[slot], kNoKey, k);
-                if (prev == kNoKey || prev == k) {
-                    atomicAdd(&scnt[slot], 1u);
-                    break;
+        // all of a thread's keys of the chunk are loaded at once (one memory latency)
+        uint32_t k[kCountPer];
+#pragma unroll
+        for (uint32_t q = 0; q < kCountPer; q++) {
+            const uint32_t i = base + q * kSampleThreads + threadIdx.x;
+            k[q] = i < end ? kw[i] : kNoKey;
+        }
+        // lanes holding the same key are counted once, by the lowest of them,
+        // so a skewed chunk's heaviest keys cost one shared atomic per warp;
+        // a slot taken for the first time is listed for the flush
+#pragma unroll
+        for (uint32_t q = 0; q < kCountPer; q++) {
+            const bool has = base + q * kSampleThreads + threadIdx.x < end;
+            const uint32_t same = __match_any_sync(0xFFFFFFFFu, k[q]) & __ballot_sync(0xFFFFFFFFu, has);
+            if (has && lane_id() == (uint32_t)(__ffs(same) - 1)) {
+                const uint32_t c = __popc(same);
+                if (k[q] == kNoKey) {
+                    if (atomicAdd(&scnt[kCountSlots], c) == 0u) used[atomicAdd(&n_used, 1u)] = (uint16_t)kCountSlots;
+                } else {
+                    uint32_t slot = slot_hash(k[q], kCountSlotsLog2);
+                    for (uint32_t p = 0; p < kCountSlots; p++) {
+                        const uint32_t prev = atomicCAS(&skey[slot], kNoKey, k[q]);
+                        if (prev == kNoKey || prev == k[q]) {
+                            if (prev == kNoKey) used[atomicAdd(&n_used, 1u)] = (uint16_t)slot;
+                            atomicAdd(&scnt[slot], c);
+                            break;
+                        }
+                        slot = (slot + 1) & (kCountSlots - 1);
+                    }
                 }
-                slot = (slot + 1) & (kCountSlots - 1);
             }
         }
         SJBG_BARRIER();
-        for (uint32_t j = threadIdx.x; j <= kCountSlots; j += blockDim.x) {
-            const uint32_t c = scnt[j];
-            if (!c) continue;
-            count_update(s, sc, hw, tw, lw, kmin, inv, j < kCountSlots ? skey[j] : kNoKey, c);
+        // one global update per distinct key of the chunk, from the list of taken slots
+        const uint32_t nu = n_used;
+        for (uint32_t u = threadIdx.x; u < nu; u += blockDim.x) {
+            const uint32_t j = used[u];
+            count_update(s, sc, hw, tw, lw, kmin, inv, j < kCountSlots ? skey[j] : kNoKey, scnt[j]);
             if (j < kCountSlots) skey[j] = kNoKey;
             scnt[j] = 0;
         }
+        SJBG_BARRIER();
+        if (threadIdx.x == 0) n_used = 0;
         SJBG_BARRIER();
     }
 }
@@ -265,6 +307,49 @@ heavy_candidates_kernel(const SampleWin *wins, const unsigned long long *table, 
     }
 }
 
+// Exclusive scan of two 64-bit values over the CTA (all threads; ends with a
+// barrier, so ws may be reused): returns the prefix of v1, stores the prefix
+// of v2 in *ex2 (when given) and both totals.
+__device__ __forceinline__ unsigned long long cta_excl_scan2(unsigned long long v1, unsigned long long v2,
+                                                             unsigned long long *tot1, unsigned long long *tot2,
+                                                             unsigned long long (*ws)[2],
+                                                             unsigned long long *ex2 = nullptr) {
+    const uint32_t lane = lane_id(), wid = warp_id(), nw = blockDim.x >> 5;
+    unsigned long long x1 = v1, x2 = v2;
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const unsigned long long y1 = __shfl_up_sync(0xFFFFFFFFu, x1, o), y2 = __shfl_up_sync(0xFFFFFFFFu, x2, o);
+        if (lane >= o) {
+            x1 += y1;
+            x2 += y2;
+        }
+    }
+    if (lane == 31) {
+        ws[wid][0] = x1;
+        ws[wid][1] = x2;
+    }
+    SJBG_BARRIER();
+    if (wid == 0) {
+        unsigned long long t1 = lane < nw ? ws[lane][0] : 0ull, t2 = lane < nw ? ws[lane][1] : 0ull;
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const unsigned long long y1 = __shfl_up_sync(0xFFFFFFFFu, t1, o), y2 = __shfl_up_sync(0xFFFFFFFFu, t2, o);
+            if (lane >= o) {
+                t1 += y1;
+                t2 += y2;
+            }
+        }
+        __syncwarp();
+        ws[lane][0] = t1;   // inclusive over warps
+        ws[lane][1] = t2;
+    }
+    SJBG_BARRIER();
+    const unsigned long long b1 = wid ? ws[wid - 1][0] : 0ull, b2 = wid ? ws[wid - 1][1] : 0ull;
+    *tot1 = ws[nw - 1][0];
+    *tot2 = ws[nw - 1][1];
+    SJBG_BARRIER();
+    if (ex2) *ex2 = b2 + x2 - v2;
+    return b1 + x1 - v1;
+}
+
 // One CTA (1024 threads) per window.
 __global__ void __launch_bounds__(1024)
 learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, unsigned long long *cand,
@@ -274,7 +359,8 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
     __shared__ float lfit[kMaxLeaves][5];          // per leaf: n, mean x, mean y, slope, largest y
     __shared__ uint32_t lstart[kMaxLeaves + 1];     // first bin of each leaf
     __shared__ uint32_t warp_tot[32];
-    __shared__ double rootpart[32][2];
+    __shared__ unsigned long long wsum[32][2];
+    __shared__ unsigned long long bsum[kMaxLeaves + 1][2];   // S1 and S2 at each leaf's first bin
     __shared__ float root_s[2];
     __shared__ uint32_t n_heavy_s, light_total_s, log2_eff_s, compact_s, cost_s;
     __shared__ uint32_t cpre[kCandMax + 1];        // exclusive prefix of the sorted candidates' counts
@@ -301,10 +387,14 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         unsigned long long v0 = sc[t], v1 = sc[t + 1024];
         // element i with partner value pv: the lower index of a descending
         // pair (and the upper of an ascending one) keeps the larger value
+        // (values are distinct keys' entries, or equal zeros of the padding)
         auto cx = [](unsigned long long v, unsigned long long pv, uint32_t i, uint32_t j, uint32_t k) {
-            const bool lower = (i & j) == 0, desc = (i & k) == 0;
-            return (lower == desc) ? (v > pv ? v : pv) : (v < pv ? v : pv);
+            const bool keep_larger = ((i & j) == 0) == ((i & k) == 0);
+            return (v > pv) == keep_larger ? v : pv;
         };
+        // up to 1,024 candidates the second elements are all padding (zeros
+        // meet only zeros): the whole CTA skips them
+        const bool two = ncap > 1024;
         for (uint32_t k = 2; k <= ncap; k <<= 1) {
             for (uint32_t j = k >> 1; j > 0; j >>= 1) {
                 if (j == 1024) {   // k = 2048: descending, element t is the lower one
@@ -313,17 +403,16 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
                     v1 = lo;
                 } else if (j >= 32) {
                     sc[t] = v0;
-                    sc[t + 1024] = v1;
+                    if (two) sc[t + 1024] = v1;
                     SJBG_BARRIER();
-                    const unsigned long long p0 = sc[t ^ j], p1 = sc[(t ^ j) + 1024];
+                    const unsigned long long p0 = sc[t ^ j];
+                    const unsigned long long p1 = two ? sc[(t ^ j) + 1024] : 0ull;
                     SJBG_BARRIER();
                     v0 = cx(v0, p0, t, j, k);
-                    v1 = cx(v1, p1, t + 1024, j, k);
+                    if (two) v1 = cx(v1, p1, t + 1024, j, k);
                 } else {
-                    const unsigned long long p0 = __shfl_xor_sync(0xFFFFFFFFu, v0, j);
-                    const unsigned long long p1 = __shfl_xor_sync(0xFFFFFFFFu, v1, j);
-                    v0 = cx(v0, p0, t, j, k);
-                    v1 = cx(v1, p1, t + 1024, j, k);
+                    v0 = cx(v0, __shfl_xor_sync(0xFFFFFFFFu, v0, j), t, j, k);
+                    if (two) v1 = cx(v1, __shfl_xor_sync(0xFFFFFFFFu, v1, j), t + 1024, j, k);
                 }
             }
         }
@@ -397,55 +486,43 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         if (placed_s[h]) atomicSub(&hb[bin_of(key_x(M.heavy_keys[h], kmin, inv))], (uint32_t)(sc[h] >> 32));
     SJBG_BARRIER();
 
-    // ---- inclusive scan: warp w owns bins [w * per, (w + 1) * per), 32 at a time
-    const uint32_t nwarps = blockDim.x >> 5, per = kBins / nwarps;
+    // ---- the light CDF at the bin edges, and its running sums, in integers.
+    // Thread t owns bins [t * pt, (t + 1) * pt).  With cdf_j the inclusive
+    // count of bin j, S1(j) = sum_{i<j} cdf_i and S2(j) = sum_{i<j} i * cdf_i
+    // are exact; every least-squares sum below is a difference of them or a
+    // closed form in the bin index, so no sum is formed in floating point.
+    const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t wid = warp_id(), lane = lane_id();
-    {
-        uint32_t carry = 0;
-        for (uint32_t b = wid * per; b < (wid + 1) * per; b += 32) {
-            const uint32_t v = hb[b + lane];
-            uint32_t tot;
-            const uint32_t ex = warp_excl_scan(v, &tot);
-            hb[b + lane] = carry + ex + v;
-            carry += tot;
-        }
-        if (lane == 0) warp_tot[wid] = carry;
+    const uint32_t pt = kBins / blockDim.x, jb = threadIdx.x * pt;
+    uint32_t cnt = 0;
+    unsigned long long a1 = 0, a2 = 0;   // the chunk's own inclusive counts: their sum, and sum j * them
+    for (uint32_t q = 0; q < pt; q++) {
+        cnt += hb[jb + q];
+        a1 += cnt;
+        a2 += (unsigned long long)(jb + q) * cnt;
     }
-    SJBG_BARRIER();
-    if (wid == 0) {
-        const uint32_t x = lane < nwarps ? warp_tot[lane] : 0u;
-        uint32_t tt;
-        const uint32_t e = warp_excl_scan(x, &tt);
-        warp_tot[lane] = e;
-        if (lane == 0) light_total_s = tt;
+    unsigned long long tot_cnt, dummy;
+    const unsigned long long before = cta_excl_scan2(cnt, 0ull, &tot_cnt, &dummy, wsum);   // counts ahead of the chunk
+    // the chunk's share of S1 and S2: every inclusive count is `before` higher than its local one
+    const unsigned long long sj = (unsigned long long)pt * jb + (unsigned long long)pt * (pt - 1) / 2;
+    unsigned long long s1k, s2k;
+    unsigned long long e1 = 0, e2 = 0;
+    e1 = cta_excl_scan2(pt * before + a1, before * sj + a2, &s1k, &s2k, wsum, &e2);
+    if (threadIdx.x == 0) light_total_s = (uint32_t)tot_cnt;
+    for (uint32_t l = threadIdx.x; l <= leaves; l += blockDim.x) {
+        lstart[l] = kBins;
+        bsum[l][0] = s1k;
+        bsum[l][1] = s2k;
     }
-    SJBG_BARRIER();
-    for (uint32_t b = wid * per; b < (wid + 1) * per; b += 32) hb[b + lane] += warp_tot[wid];
     SJBG_BARRIER();
     const uint32_t total = light_total_s;
     const float invt = total ? 1.0f / (float)total : 0.0f;
 
-    // ---- root line y = a x + b over the bin points x_j = (j + 1) / kBins, y_j = cdf_j;
-    // sum x and sum x^2 are closed forms, sum y and sum x*y are reduced per warp in double
-    {
-        float sy = 0.f, sxy = 0.f;
-        for (uint32_t j = threadIdx.x; j < kBins; j += blockDim.x) {
-            const float y = (float)hb[j] * invt;
-            sy += y;
-            sxy += y * ((float)(j + 1) / (float)kBins);
-        }
-        double dy = sy, dxy = sxy;
-        for (int o = 16; o > 0; o >>= 1) {
-            dy += __shfl_xor_sync(0xFFFFFFFFu, dy, o);
-            dxy += __shfl_xor_sync(0xFFFFFFFFu, dxy, o);
-        }
-        if (lane == 0) { rootpart[wid][0] = dy; rootpart[wid][1] = dxy; }
-    }
-    SJBG_BARRIER();
+    // ---- root line y = a x + b over the bin points x_j = (j + 1) / kBins, y_j = cdf_j / total:
+    // sum x and sum x^2 are closed forms, sum y = S1(K) / total, sum x y = (S2(K) + S1(K)) / (K total)
     if (threadIdx.x == 0) {
-        double sy = 0.0, sxy = 0.0;
-        for (uint32_t q = 0; q < nwarps; q++) { sy += rootpart[q][0]; sxy += rootpart[q][1]; }
-        const double nn = kBins;
+        const double nn = kBins, it = total ? 1.0 / (double)total : 0.0;
+        const double sy = (double)s1k * it, sxy = ((double)s2k + (double)s1k) * it / nn;
         const double sx = (nn + 1.0) / 2.0, sxx = (nn + 1.0) * (2.0 * nn + 1.0) / (6.0 * nn);
         const double den = nn * sxx - sx * sx;
         double ra = den != 0.0 ? (nn * sxy - sx * sy) / den : 1.0;
@@ -453,7 +530,6 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         root_s[0] = (float)ra;
         root_s[1] = (float)((sy - ra * sx) / nn);
     }
-    for (uint32_t l = threadIdx.x; l <= leaves; l += blockDim.x) lstart[l] = kBins;
     SJBG_BARRIER();
     const float root_a = root_s[0], root_b = root_s[1];
     auto leaf_of = [&](uint32_t j) {
@@ -461,52 +537,56 @@ learned_fit_kernel(const SampleWin *wins, SampleScratch *scr, uint32_t *hist, un
         int l = (int)floorf((root_a * x + root_b) * (float)leaves);
         return min(max(l, 0), (int)leaves - 1);
     };
-    // leaf_of is non-decreasing in j, so every leaf owns a contiguous run of bins:
-    // the first bin of leaf l is where leaf_of first reaches l
-    for (uint32_t j = threadIdx.x; j < kBins; j += blockDim.x) {
-        const int lj = leaf_of(j);
-        const int lp = j ? leaf_of(j - 1) : -1;
-        for (int l = lp + 1; l <= lj; l++) lstart[l] = j;
+    // leaf_of is non-decreasing in j, so every leaf owns a contiguous run of
+    // bins: the first bin of leaf l is where leaf_of first reaches l.  The
+    // owner of that bin records it with S1 and S2 there, and stores its CDF.
+    {
+        unsigned long long s1 = e1, s2 = e2;
+        uint32_t run = before;
+        int lp = jb ? leaf_of(jb - 1) : -1;
+        for (uint32_t q = 0; q < pt; q++) {
+            const uint32_t j = jb + q;
+            const int lj = leaf_of(j);
+            for (int l = lp + 1; l <= lj; l++) {
+                lstart[l] = j;
+                bsum[l][0] = s1;
+                bsum[l][1] = s2;
+            }
+            lp = lj;
+            run += hb[j];
+            hb[j] = run;
+            s1 += run;
+            s2 += (unsigned long long)j * run;
+        }
     }
     SJBG_BARRIER();
 
-    // ---- one warp per leaf: centred least-squares line over the leaf's bins
-    for (uint32_t l = wid; l < leaves; l += nwarps) {
+    // ---- one thread per leaf: least-squares line over the leaf's bins [j0, j1),
+    // centred at the leaf's mean x.  With c = j1 - j0 bins:
+    //   mean x = (j0 + j1 + 1) / 2K,  sum dx^2 = c (c^2 - 1) / 12K^2,
+    //   sum dx dy = sum dx y = (2 S2 - (j0 + j1 - 1) S1) / (2K total)  (S1, S2 over the leaf)
+    for (uint32_t l = threadIdx.x; l < leaves; l += blockDim.x) {
         const uint32_t j0 = lstart[l], j1 = lstart[l + 1];
-        float c = 0.f, sx = 0.f, sy = 0.f, mxv = -1.f;
-        for (uint32_t j = j0 + lane; j < j1; j += 32) {
-            const float y = (float)hb[j] * invt;
-            c += 1.f;
-            sx += (float)(j + 1) / (float)kBins;
-            sy += y;
-            mxv = fmaxf(mxv, y);
+        const uint32_t c = j1 > j0 ? j1 - j0 : 0u;
+        float mx = 0.f, my = 0.f, slope = 0.f, mxv = -1.f;
+        if (c) {
+            const unsigned long long s1 = bsum[l + 1][0] - bsum[l][0];
+            const long long s2 = (long long)(bsum[l + 1][1] - bsum[l][1]);
+            const long long t = 2 * s2 - (long long)(j0 + j1 - 1) * (long long)s1;
+            mx = (float)(j0 + j1 + 1) / (2.0f * (float)kBins);
+            my = (float)s1 * invt / (float)c;
+            mxv = (float)hb[j1 - 1] * invt;   // the CDF does not decrease: its value at the last bin
+            if (c > 1) {
+                const float fc = (float)c;
+                slope = 6.0f * (float)kBins * invt * (float)t / (fc * (fc * fc - 1.0f));
+                if (!(slope >= 0.f)) slope = 0.f;
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
-            sx += __shfl_xor_sync(0xFFFFFFFFu, sx, o);
-            sy += __shfl_xor_sync(0xFFFFFFFFu, sy, o);
-            mxv = fmaxf(mxv, __shfl_xor_sync(0xFFFFFFFFu, mxv, o));
-        }
-        const float mx = c > 0.f ? sx / c : 0.f, my = c > 0.f ? sy / c : 0.f;
-        float sxy = 0.f, sxx = 0.f;
-        for (uint32_t j = j0 + lane; j < j1; j += 32) {
-            const float dx = (float)(j + 1) / (float)kBins - mx, dy = (float)hb[j] * invt - my;
-            sxy += dx * dy;
-            sxx += dx * dx;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            sxy += __shfl_xor_sync(0xFFFFFFFFu, sxy, o);
-            sxx += __shfl_xor_sync(0xFFFFFFFFu, sxx, o);
-        }
-        if (lane == 0) {
-            float slope = sxx > 0.f ? sxy / sxx : 0.f;
-            if (!(slope >= 0.f)) slope = 0.f;
-            lfit[l][0] = c;
-            lfit[l][1] = mx;
-            lfit[l][2] = my;
-            lfit[l][3] = slope;
-            lfit[l][4] = c > 0.f ? mxv : -1.f;   // largest CDF value routed to the leaf
-        }
+        lfit[l][0] = (float)c;
+        lfit[l][1] = mx;
+        lfit[l][2] = my;
+        lfit[l][3] = slope;
+        lfit[l][4] = mxv;   // largest CDF value routed to the leaf (-1 when empty)
     }
     SJBG_BARRIER();
     // ---- monotone clamps: a leaf owns the CDF range from the largest value of
@@ -562,11 +642,18 @@ learned_check_kernel(const uint32_t *keys, const SampleWin *wins, const LearnedM
     uint32_t *rw = prad + (uint64_t)w * kPredStride;
     const uint32_t *kw = keys + s.key_off;
     const uint32_t rmask = (1u << s.log2_buckets) - 1u;   // radix on the plan's fan-out, every key
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.m; i += gridDim.x * blockDim.x) {
-        const uint32_t k = kw[i];
-        if (core.cost_check) atomicAdd(&rw[k & rmask], 1u);
-        if (heavy_find(hs, k) != kHeavyBucket) continue;
-        atomicAdd(&pw[learned_bucket(core, k)], 1u);
+    // four keys per thread loaded at once (one memory latency per four keys)
+    const uint32_t step = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < s.m; i0 += 4 * step) {
+        uint32_t k[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) k[q] = i0 + q * step < s.m ? kw[i0 + q * step] : 0u;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (i0 + q * step >= s.m) continue;
+            if (core.cost_check) atomicAdd(&rw[k[q] & rmask], 1u);
+            if (heavy_find(hs, k[q]) == kHeavyBucket) atomicAdd(&pw[learned_bucket(core, k[q])], 1u);
+        }
     }
 }
 
@@ -656,6 +743,9 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         s.list_off = list_total;
         list_total += s.list_cap;
         s.pad = 0;
+        const uint64_t runs = m >> (s.run_log2 + 1);   // runs per side
+        s.stride[0] = runs ? p.n_left / runs : 0;
+        s.stride[1] = runs ? p.n_right / runs : 0;
         max_m = std::max(max_m, s.m);
         max_list = std::max(max_list, s.list_cap);
     }
