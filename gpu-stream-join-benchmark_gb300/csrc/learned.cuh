@@ -22,7 +22,7 @@
 namespace sjbg {
 
 constexpr uint32_t kMaxLeaves = 256;
-constexpr uint32_t kMaxHeavy = 512;
+constexpr uint32_t kMaxHeavy = 1024;
 constexpr uint32_t kHeavySlotsLog2 = 12;
 constexpr uint32_t kHeavySlots = 1u << kHeavySlotsLog2;   // shared-memory heavy-key table
 constexpr uint32_t kHeavyBucketsLog2 = kHeavySlotsLog2 - 1;   // buckets of two slots (16 bytes)
