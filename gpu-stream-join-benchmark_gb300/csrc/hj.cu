@@ -1463,9 +1463,11 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     for (uint32_t w = 0; w < n; w++)
         for (uint32_t k = 0; k < (1u << plan[w].log2_buckets); k++) bwin[plan[w].bucket_base + k] = w;
 
-    // ---- upload plan, tile prefixes and bucket->window map in one copy
+    // ---- upload plan, tile prefixes, bucket->window map and (learned) the
+    // sampling plan in one copy
     const size_t planB = sizeof(WinPlan) * n, tileB = sizeof(uint32_t) * (n + 1), bwB = sizeof(uint32_t) * B;
-    const size_t upB = planB + 8 * tileB + bwB;
+    const size_t lsOff = (planB + 8 * tileB + bwB + 15) & ~(size_t)15;
+    const size_t upB = lsOff + (learned ? learned_stage_bytes(n) : 0);
     uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 0, upB));
     uint8_t *dev = static_cast<uint8_t *>(ws_get(h, WS_WIN_PLAN, upB));
     if (!hst || !dev) return fail(h, SJBG_E_NOMEM, "plan buffers");
@@ -1479,6 +1481,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     std::memcpy(hst + planB + 6 * tileB, pbL.data(), tileB);
     std::memcpy(hst + planB + 7 * tileB, pbR.data(), tileB);
     std::memcpy(hst + planB + 8 * tileB, bwin.data(), bwB);
+    LearnedStage lst{};
+    if (learned) lst = learned_stage(h, plan.data(), n, hst + lsOff);
     if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
     WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
     const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
@@ -1501,7 +1505,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     const LearnedModel *dModels = nullptr;
     HeavyAcc *dHeavy = nullptr;
     if (learned) {
-        int rc = learned_prepare(h, dL, dR, plan.data(), n, dPlan, &dModels, !enumerate);
+        int rc = learned_prepare(h, dL, dR, lst, dev + lsOff, n, dPlan, &dModels, !enumerate);
         if (rc) return rc;
         dHeavy = static_cast<HeavyAcc *>(ws_get(h, WS_HEAVY, sizeof(HeavyAcc) * kMaxHeavy * n));
         if (!dHeavy) return fail(h, SJBG_E_NOMEM, "heavy-key accumulators");

@@ -704,17 +704,16 @@ uint32_t learned_log2_buckets(sjbg_handle *h, uint64_t n_left) {
     return b;
 }
 
-int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinPlan *plan, uint32_t n,
-                    WinPlan *dPlan, const LearnedModel **dModels, bool allow_heavy) {
+size_t learned_stage_bytes(uint32_t n) { return (sizeof(SampleWin) + sizeof(SampleScratch)) * (size_t)n; }
+
+LearnedStage learned_stage(sjbg_handle *h, const WinPlan *plan, uint32_t n, uint8_t *hst) {
     const float rate = h->cfg.sample_rate > 0.0f ? h->cfg.sample_rate : 0.01f;
-    const float bound = h->cfg.overflow_bound > 0.0f ? h->cfg.overflow_bound : 8.0f;
-    const uint32_t leaves = h->cfg.learned_leaves ? std::min(h->cfg.learned_leaves, kMaxLeaves) : kMaxLeaves;
-    std::vector<SampleWin> sw(n);
-    uint64_t table_total = 0, keys_total = 0, list_total = 0;
-    uint32_t max_m = 0, max_list = 0;
+    LearnedStage st{};
+    SampleWin *sw = reinterpret_cast<SampleWin *>(hst);
     for (uint32_t w = 0; w < n; w++) {
         const WinPlan &p = plan[w];
-        SampleWin &s = sw[w];
+        SampleWin s;
+        std::memset(&s, 0, sizeof(s));
         s.left_off = p.left_off; s.n_left = p.n_left; s.right_off = p.right_off; s.n_right = p.n_right;
         const uint64_t nmin = std::min(p.n_left, p.n_right);
         uint64_t m = (uint64_t)((double)rate * (double)(p.n_left + p.n_right));
@@ -723,37 +722,48 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
         // runs of 8 tuples (whole 128-byte lines) once each side has room for
         // 8 runs: m a multiple of 16 samples, at most one per tuple
         s.run_log2 = (m >= 128 && nmin >= 64) ? 3u : 0u;
-        s.pad0 = 0;
         m &= ~((2ull << s.run_log2) - 1);
         if (nmin == 0) m = 0;
         s.m = (uint32_t)m;
         uint32_t lg = 6;
         while (((uint64_t)1 << lg) < 2 * m) lg++;
         s.table_log2 = lg;
-        s.table_off = table_total;
-        table_total += (uint64_t)1 << lg;
+        s.table_off = st.table_total;
+        st.table_total += (uint64_t)1 << lg;
         s.log2_buckets = p.log2_buckets;
         const uint64_t P = (uint64_t)1 << p.log2_buckets;
         // heavy candidates: keys sampled at least max(4, m / 64P) times; the fit
         // keeps those that exceed an eighth of a bucket of the remaining light mass
         s.thresh = (uint32_t)std::max<uint64_t>(4, m / (64 * P));
-        s.key_off = keys_total;
-        keys_total += m;
+        s.key_off = st.keys_total;
+        st.keys_total += m;
         s.list_cap = (uint32_t)(m / s.thresh + 1);
-        s.list_off = list_total;
-        list_total += s.list_cap;
-        s.pad = 0;
+        s.list_off = st.list_total;
+        st.list_total += s.list_cap;
         const uint64_t runs = m >> (s.run_log2 + 1);   // runs per side
         s.stride[0] = runs ? p.n_left / runs : 0;
         s.stride[1] = runs ? p.n_right / runs : 0;
-        max_m = std::max(max_m, s.m);
-        max_list = std::max(max_list, s.list_cap);
+        st.max_m = std::max(st.max_m, s.m);
+        st.max_list = std::max(st.max_list, s.list_cap);
+        std::memcpy(&sw[w], &s, sizeof(s));
     }
-    const size_t swB = sizeof(SampleWin) * n, scB = sizeof(SampleScratch) * n;
+    SampleScratch init;
+    std::memset(&init, 0, sizeof(init));
+    init.kmin = 0xFFFFFFFFu;
+    for (uint32_t w = 0; w < n; w++) std::memcpy(hst + sizeof(SampleWin) * n + sizeof(SampleScratch) * w, &init, sizeof(init));
+    return st;
+}
+
+int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const LearnedStage &st,
+                    uint8_t *dstage, uint32_t n, WinPlan *dPlan, const LearnedModel **dModels, bool allow_heavy) {
+    const float bound = h->cfg.overflow_bound > 0.0f ? h->cfg.overflow_bound : 8.0f;
+    const uint32_t leaves = h->cfg.learned_leaves ? std::min(h->cfg.learned_leaves, kMaxLeaves) : kMaxLeaves;
+    const uint64_t table_total = st.table_total, keys_total = st.keys_total, list_total = st.list_total;
+    const uint32_t max_m = st.max_m, max_list = st.max_list;
+    const size_t swB = sizeof(SampleWin) * n;
+    uint8_t *dsmall = dstage;
     const size_t histB = sizeof(uint32_t) * (size_t)kBins * n, tabB = sizeof(unsigned long long) * table_total;
     const size_t candB = sizeof(unsigned long long) * (size_t)kCandMax * n, predB = sizeof(uint32_t) * (size_t)n * kPredStride;
-    uint8_t *hst = static_cast<uint8_t *>(pinned_get(h, 1, swB + scB));
-    uint8_t *dsmall = static_cast<uint8_t *>(ws_get(h, WS_SAMPLE, swB + scB));
     // sample histograms, then the model's and radix's predicted bucket counts
     uint32_t *dHist = static_cast<uint32_t *>(ws_get(h, WS_AUX0, histB + 2 * predB));
     unsigned long long *dTab = static_cast<unsigned long long *>(ws_get(h, WS_AUX1, tabB));
@@ -761,18 +771,11 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     LearnedModel *dM = static_cast<LearnedModel *>(ws_get(h, WS_MODEL, sizeof(LearnedModel) * n));
     // the packed sample keys of every window, then the windows' lists of keys at or above thresh
     uint32_t *dKeys = static_cast<uint32_t *>(ws_get(h, WS_SAMPLE_KEYS, sizeof(uint32_t) * (keys_total + list_total + 1)));
-    if (!hst || !dsmall || !dHist || !dTab || !dCand || !dM || !dKeys)
+    if (!dHist || !dTab || !dCand || !dM || !dKeys)
         return fail(h, SJBG_E_NOMEM, "learned partitioner buffers");
     uint32_t *dLists = dKeys + keys_total;
     uint32_t *dPred = dHist + (size_t)kBins * n;
     uint32_t *dPrad = dPred + (size_t)n * kPredStride;
-    std::memcpy(hst, sw.data(), swB);
-    SampleScratch init;
-    std::memset(&init, 0, sizeof(init));
-    init.kmin = 0xFFFFFFFFu;
-    std::vector<SampleScratch> scr(n, init);
-    std::memcpy(hst + swB, scr.data(), scB);
-    if (int rc_up = stage_copy(h, dsmall, hst, swB + scB)) return rc_up;
     SJBG_CK(h, cudaMemsetAsync(dHist, 0, histB + 2 * predB, h->stream));
     SJBG_CK(h, cudaMemsetAsync(dTab, 0, tabB, h->stream));
     const SampleWin *dSw = reinterpret_cast<const SampleWin *>(dsmall);
@@ -782,7 +785,17 @@ int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     const uint32_t bs = std::max<uint32_t>(1, std::min<uint32_t>(256, (max_m + 1023) / 1024));
     SJBG_CK(h, launch(h, "learned_sample", sample_minmax_kernel, dim3(bs, n), dim3(kSampleThreads), 0, dL, dR, dSw,
                       dScr, dKeys));
-    const uint32_t bn = std::max<uint32_t>(1, std::min<uint32_t>(256, (max_m + kCountChunk - 1) / kCountChunk));
+    // one chunk per CTA, unless the CTAs of all windows would take more than
+    // one wave: then each CTA takes several chunks in turn (a second wave
+    // costs a whole CTA's latency, a second chunk less)
+    int count_per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&count_per_sm, sample_count_kernel, kSampleThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        count_per_sm = 1;
+    }
+    const uint32_t wave = (uint32_t)std::max(count_per_sm, 1) * (uint32_t)std::max(h->num_sms, 1);
+    const uint32_t bn = std::max<uint32_t>(1, std::min<uint32_t>({256u, (max_m + kCountChunk - 1) / kCountChunk,
+                                                                  std::max<uint32_t>(1, wave / std::max<uint32_t>(n, 1))}));
     SJBG_CK(h, launch(h, "learned_count", sample_count_kernel, dim3(bn, n), dim3(kSampleThreads), 0,
                       (const uint32_t *)dKeys, dSw, dScr, dHist, dTab, dLists));
     const uint32_t tx = std::max<uint32_t>(1, std::min<uint32_t>(16, (max_list + 4095) / 4096));

@@ -145,9 +145,19 @@ struct sjbg_handle;
 namespace sjbg {
 struct WinPlan;
 uint32_t learned_log2_buckets(sjbg_handle *h, uint64_t n_left);
-// Sample, fit and check every window's model; writes models and sets
-// WinPlan::model on device (dPlan) for the windows that keep their model.
-// allow_heavy = false keeps every key in the partitions (needed when pairs are enumerated).
-int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const WinPlan *plan, uint32_t n,
-                    WinPlan *dPlan, const LearnedModel **dModels, bool allow_heavy);
+// Sizes of the sampling buffers, from the windows' plans.
+struct LearnedStage {
+    uint64_t table_total, keys_total, list_total;
+    uint32_t max_m, max_list;
+};
+// Host bytes the sampling plan of n windows takes (uploaded with the batch plan).
+size_t learned_stage_bytes(uint32_t n);
+// Writes the sampling plan of n windows (learned_stage_bytes(n) bytes) to hst.
+LearnedStage learned_stage(sjbg_handle *h, const WinPlan *plan, uint32_t n, uint8_t *hst);
+// Sample, fit and check every window's model from the uploaded sampling plan
+// (dstage, on the device); writes models and sets WinPlan::model on device
+// (dPlan) for the windows that keep their model.  allow_heavy = false keeps
+// every key in the partitions (needed when pairs are enumerated).
+int learned_prepare(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, const LearnedStage &st,
+                    uint8_t *dstage, uint32_t n, WinPlan *dPlan, const LearnedModel **dModels, bool allow_heavy);
 }  // namespace sjbg
