@@ -509,16 +509,25 @@ __global__ void __launch_bounds__(1024) part_scan_kernel(const uint32_t *__restr
     }
 }
 
+// One bucket of the join list with what its join reads before the tuples:
+// both sides' counts and run starts, the window, the window's radix bits, and
+// whether the window is radix-partitioned (its buckets may use a direct table).
+struct __align__(16) JoinItem {
+    uint32_t b, nR, nS, sR, sS, w, lg, direct;
+};
+static_assert(sizeof(JoinItem) == 32, "two 16-byte words per join item");
+
 // Per window, one CTA: exclusive scan of the window's bucket counts on each
 // side, starting at the window's base in that side's partitioned array (the
 // tuples of the windows before it: baseL / baseR), giving the bucket starts
 // and scatter cursors; then every bucket with tuples on both sides is appended
-// to the join list (jlist, length *jn: nothing else can match).
+// to the join list (items, length *jn: nothing else can match).
 __global__ void __launch_bounds__(1024)
 part_scan_win_kernel(const WinPlan *__restrict__ wins, const uint32_t *__restrict__ baseL,
                      const uint32_t *__restrict__ baseR, const uint32_t *__restrict__ cnt,
                      uint32_t *__restrict__ start, uint32_t *__restrict__ cursor, uint32_t B,
-                     uint32_t *__restrict__ jlist, uint32_t *__restrict__ jn) {
+                     const LearnedModel *__restrict__ models, JoinItem *__restrict__ items,
+                     uint32_t *__restrict__ jn) {
     __shared__ uint32_t warp_tot[32];
     __shared__ uint32_t carry_s;
     const uint32_t w = blockIdx.x;
@@ -563,15 +572,23 @@ part_scan_win_kernel(const WinPlan *__restrict__ wins, const uint32_t *__restric
             SJBG_BARRIER();
         }
     }
-    // join list: one reservation per warp of joinable buckets
+    // join list: one reservation per warp of joinable buckets (the starts were
+    // written by this CTA, before the scan's last barrier)
+    const uint32_t direct = (models ? model_of(wp, models) : nullptr) == nullptr ? 1u : 0u;
     for (uint32_t i0 = 0; i0 < P; i0 += blockDim.x) {
         const uint32_t i = i0 + threadIdx.x, b = b0 + i;
-        const bool ok = i < P && cnt[b] != 0u && cnt[B + b] != 0u;
+        const uint32_t nR = i < P ? cnt[b] : 0u, nS = i < P ? cnt[B + b] : 0u;
+        const bool ok = nR != 0u && nS != 0u;
         const unsigned m = __ballot_sync(0xFFFFFFFFu, ok);
         uint32_t wbase = 0;
         if (lane_id() == 0 && m) wbase = atomicAdd(jn, (uint32_t)__popc(m));
         wbase = __shfl_sync(0xFFFFFFFFu, wbase, 0);
-        if (ok) jlist[wbase + __popc(m & ((1u << lane_id()) - 1u))] = b;
+        if (ok) {
+            JoinItem ji;
+            ji.b = b; ji.nR = nR; ji.nS = nS; ji.sR = start[b]; ji.sS = start[B + b];
+            ji.w = w; ji.lg = wp.log2_buckets; ji.direct = direct;
+            items[wbase + __popc(m & ((1u << lane_id()) - 1u))] = ji;
+        }
     }
 }
 
@@ -986,17 +1003,15 @@ __device__ __forceinline__ int ct_lookup(const CountTable &t, uint32_t key) {
 
 constexpr int kJoinPer = 8;   // elements per thread per tile (independent loads in flight)
 
-__device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restrict__ partL,
-                                                  const uint64_t *__restrict__ partR,
-                                                  const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt,
-                                                  uint32_t B, const uint32_t *__restrict__ bucket_win,
-                                                  WinAcc *__restrict__ acc, uint32_t cap) {
+__device__ __forceinline__ void join_count_bucket(const JoinItem &ji, uint64_t *__restrict__ partL,
+                                                  const uint64_t *__restrict__ partR, WinAcc *__restrict__ acc,
+                                                  uint32_t cap) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t novf;
-    const uint32_t nR = cnt[b], nS = cnt[B + b];
+    const uint32_t nR = ji.nR, nS = ji.nS;
     if (nR == 0 || nS == 0) return;
-    uint64_t *Rb = partL + start[b];
-    const uint64_t *Sb = partR + start[B + b];
+    uint64_t *Rb = partL + ji.sR;
+    const uint64_t *Sb = partR + ji.sS;
     // the table holds at most nR distinct keys: 2 slots per left tuple (at
     // least 64, at most the launch's capacity of 1.3 per target tuple, which
     // lets two CTAs share an SM), so buckets under the target probe at load
@@ -1062,7 +1077,7 @@ __device__ __forceinline__ void join_count_bucket(uint32_t b, uint64_t *__restri
         SJBG_BARRIER();
         if (n == 0) break;
     }
-    flush_acc(&acc[bucket_win[b]], count, 0, prod);
+    flush_acc(&acc[ji.w], count, 0, prod);
 }
 
 // ---- direct-addressed bucket join (radix windows)
@@ -1087,19 +1102,17 @@ constexpr size_t kDirectBytes = (sizeof(unsigned long long) + sizeof(uint32_t)) 
 // `clean`: the leading table entries known to be zero (CTA-uniform); a direct
 // bucket leaves the table zero again, a hash-table bucket does not.  Returns
 // false when the bucket's key range is too wide (the table is left zero).
-__device__ __forceinline__ bool join_count_direct(uint32_t b, const uint64_t *__restrict__ partL,
-                                                  const uint64_t *__restrict__ partR,
-                                                  const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt,
-                                                  uint32_t B, const uint32_t *__restrict__ bucket_win,
-                                                  WinAcc *__restrict__ acc, uint32_t lg, uint32_t &clean) {
+__device__ __forceinline__ bool join_count_direct(const JoinItem &ji, const uint64_t *__restrict__ partL,
+                                                  const uint64_t *__restrict__ partR, WinAcc *__restrict__ acc,
+                                                  uint32_t &clean) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     __shared__ uint32_t maxidx_s;
-    const uint32_t nR = cnt[b], nS = cnt[B + b];
+    const uint32_t nR = ji.nR, nS = ji.nS, lg = ji.lg;
     if (nR == 0 || nS == 0) return true;
     unsigned long long *dsum = reinterpret_cast<unsigned long long *>(smem_raw);
     uint32_t *dcnt = reinterpret_cast<uint32_t *>(dsum + kDirectMax);
-    const uint64_t *Rb = partL + start[b];
-    const uint64_t *Sb = partR + start[B + b];
+    const uint64_t *Rb = partL + ji.sR;
+    const uint64_t *Sb = partR + ji.sS;
     for (uint32_t i = clean + threadIdx.x; i < kDirectMax; i += blockDim.x) {
         dsum[i] = 0;
         dcnt[i] = 0;
@@ -1184,7 +1197,7 @@ __device__ __forceinline__ bool join_count_direct(uint32_t b, const uint64_t *__
         }
         SJBG_BARRIER();
     }
-    flush_acc(&acc[bucket_win[b]], count, 0, prod);
+    flush_acc(&acc[ji.w], count, 0, prod);
     return true;
 }
 
@@ -1298,41 +1311,84 @@ __device__ __forceinline__ void join_enum_bucket(uint32_t b, const uint64_t *__r
     flush_acc(&acc[w], count, xr, prod);
 }
 
-// Bucket joins over the join list (jlist, length *jn; or, without a list,
-// buckets 0 .. B-1): one CTA per item (queue == nullptr) or persistent CTAs
-// that take items from a device work queue (an atomic counter) until it runs dry.
-// With wins (null: hash tables only), the buckets of radix windows are joined
-// through direct tables when their key indices allow it.
+// Bucket joins over the join list (items, length *jn; or, without a list,
+// buckets 0 .. B-1, hash tables only): one CTA per item (queue == nullptr) or
+// persistent CTAs that take items from a device work queue (an atomic counter)
+// until it runs dry.  Buckets of radix windows are joined through direct
+// tables when their key indices allow it.
+//
+// A persistent CTA works one item ahead: while it joins item k, item k+1's
+// record is already in shared memory and its two runs are being prefetched
+// into L2, and item k+2's record is on its way (an asynchronous copy into
+// shared memory, from the index claimed during item k-1).  So no step of a
+// bucket waits on the queue, the list or the first loads of its runs.
 __global__ void __launch_bounds__(kJoinThreads)
 bucket_join_count_kernel(uint64_t *__restrict__ partL, const uint64_t *__restrict__ partR,
                          const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
                          const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc, uint32_t cap,
-                         uint32_t *queue, const uint32_t *__restrict__ jlist, const uint32_t *__restrict__ jn,
-                         const WinPlan *__restrict__ wins, const LearnedModel *__restrict__ models) {
-    const uint32_t items = jlist ? *jn : B;
+                         uint32_t *queue, const JoinItem *__restrict__ items, const uint32_t *__restrict__ jn) {
+    const uint32_t nitems = items ? *jn : B;
     uint32_t clean = 0;
-    auto join = [&](uint32_t b) {
-        if (wins) {
-            const WinPlan &wp = wins[bucket_win[b]];
-            if (!model_of(wp, models) && cnt[b] + cnt[B + b] <= kDirectMaxRun &&
-                join_count_direct(b, partL, partR, start, cnt, B, bucket_win, acc, wp.log2_buckets, clean))
-                return;
-        }
-        join_count_bucket(b, partL, partR, start, cnt, B, bucket_win, acc, cap);
+    auto join = [&](const JoinItem &ji) {
+        if (ji.direct && ji.nR + ji.nS <= kDirectMaxRun && join_count_direct(ji, partL, partR, acc, clean)) return;
+        join_count_bucket(ji, partL, partR, acc, cap);
         clean = 0;
     };
-    if (!queue) {
-        if (blockIdx.x < items) join(jlist ? jlist[blockIdx.x] : blockIdx.x);
+    if (!queue || !items) {
+        if (blockIdx.x >= nitems) return;
+        JoinItem ji;
+        if (items) {
+            ji = items[blockIdx.x];
+        } else {
+            const uint32_t i = blockIdx.x;
+            ji.b = i; ji.nR = cnt[i]; ji.nS = cnt[B + i]; ji.sR = start[i]; ji.sS = start[B + i];
+            ji.w = bucket_win[i]; ji.lg = 0; ji.direct = 0;
+        }
+        join(ji);
         return;
     }
-    __shared__ uint32_t item_s;
-    for (;;) {
+    __shared__ JoinItem slot_s[3];   // item k, k+1, k+2 (by position: cur_s, then the two ahead)
+    __shared__ uint32_t cur_s, valid_s;   // slot of item k; bit q: slot (cur + q) % 3 holds an item
+    uint32_t claim = 0;                   // thread 0: index claimed for item k+2
+    if (threadIdx.x == 0) {
+        const uint32_t i0 = atomicAdd(queue, 1u), i1 = atomicAdd(queue, 1u);
+        if (i0 < nitems) slot_s[0] = items[i0];
+        if (i1 < nitems) slot_s[1] = items[i1];
+        cur_s = 0;
+        valid_s = (i0 < nitems ? 1u : 0u) | (i1 < nitems ? 2u : 0u);
+        claim = atomicAdd(queue, 1u);
+    }
+    SJBG_BARRIER();
+    while (valid_s & 1u) {
+        const uint32_t c = cur_s, v = valid_s;
+        const JoinItem ji = slot_s[c];
+        const uint32_t c1 = c == 2 ? 0u : c + 1u, c2 = c1 == 2 ? 0u : c1 + 1u;
+        uint32_t claim_next = 0;
+        if (threadIdx.x == 0) {
+            if (v & 2u) {   // item k+1: its runs into L2 while item k is joined
+                const JoinItem &nx = slot_s[c1];
+                l2_prefetch_bulk(partL + nx.sR, sizeof(uint64_t) * nx.nR);
+                l2_prefetch_bulk(partR + nx.sS, sizeof(uint64_t) * nx.nS);
+            }
+            if (claim < nitems) {   // item k+2's record: shared memory, without blocking
+                const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&slot_s[c2]);
+                const JoinItem *src = items + claim;
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n"
+                             "cp.async.cg.shared.global [%2], [%3], 16;\n"
+                             "cp.async.commit_group;\n" ::"r"(dst), "l"(src), "r"(dst + 16u),
+                             "l"(reinterpret_cast<const uint8_t *>(src) + 16)
+                             : "memory");
+            }
+            claim_next = atomicAdd(queue, 1u);   // read after this item's join
+        }
+        join(ji);
+        if (threadIdx.x == 0) {
+            asm volatile("cp.async.wait_all;\n" ::: "memory");
+            cur_s = c1;
+            valid_s = (v >> 1) | (claim < nitems ? 2u : 0u);
+            claim = claim_next;
+        }
         SJBG_BARRIER();
-        if (threadIdx.x == 0) item_s = atomicAdd(queue, 1u);
-        SJBG_BARRIER();
-        const uint32_t it = item_s;
-        if (it >= items) break;
-        join(jlist ? jlist[it] : it);
     }
 }
 
@@ -1341,12 +1397,12 @@ bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__re
                         const uint32_t *__restrict__ start, const uint32_t *__restrict__ cnt, uint32_t B,
                         const uint32_t *__restrict__ bucket_win, WinAcc *__restrict__ acc,
                         const WinPlan *__restrict__ wins, sjbg_pair *__restrict__ pairs, uint32_t table_bits,
-                        uint32_t *queue, const uint32_t *__restrict__ jlist, const uint32_t *__restrict__ jn) {
-    const uint32_t items = jlist ? *jn : B;
+                        uint32_t *queue, const JoinItem *__restrict__ jitems, const uint32_t *__restrict__ jn) {
+    const uint32_t items = jitems ? *jn : B;
     if (!queue) {
         if (blockIdx.x < items)
-            join_enum_bucket(jlist ? jlist[blockIdx.x] : blockIdx.x, partL, partR, start, cnt, B, bucket_win, acc,
-                             wins, pairs, table_bits);
+            join_enum_bucket(jitems ? jitems[blockIdx.x].b : blockIdx.x, partL, partR, start, cnt, B, bucket_win,
+                             acc, wins, pairs, table_bits);
         return;
     }
     __shared__ uint32_t item_s;
@@ -1356,7 +1412,7 @@ bucket_join_enum_kernel(const uint64_t *__restrict__ partL, const uint64_t *__re
         SJBG_BARRIER();
         const uint32_t it = item_s;
         if (it >= items) break;
-        join_enum_bucket(jlist ? jlist[it] : it, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs,
+        join_enum_bucket(jitems ? jitems[it].b : it, partL, partR, start, cnt, B, bucket_win, acc, wins, pairs,
                          table_bits);
     }
 }
@@ -1520,9 +1576,11 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     // per window side its compacted light tuples, then the join list's length
     uint32_t *dCcnt = static_cast<uint32_t *>(ws_get(h, WS_COMPACT_CNT, sizeof(uint32_t) * (2 * n + 1)));
     uint32_t *dJn = dCcnt + 2 * n;
-    // the passes' work prefixes (6 arrays of n + 1), then the join list (B)
-    uint32_t *dWork = static_cast<uint32_t *>(ws_get(h, WS_TILE_PREFIX, sizeof(uint32_t) * (6 * (n + 1) + B)));
-    uint32_t *dJlist = dWork ? dWork + 6 * (n + 1) : nullptr;
+    // the passes' work prefixes (6 arrays of n + 1), then (16-byte aligned) the join list (B items)
+    const size_t workWords = (6 * (size_t)(n + 1) + 3) & ~(size_t)3;
+    uint32_t *dWork = static_cast<uint32_t *>(
+        ws_get(h, WS_TILE_PREFIX, sizeof(uint32_t) * workWords + sizeof(JoinItem) * (size_t)std::max<uint64_t>(B, 1)));
+    JoinItem *dJlist = dWork ? reinterpret_cast<JoinItem *>(dWork + workWords) : nullptr;
     if (!dComp || !dRows || !dCcnt || !dWork) return fail(h, SJBG_E_NOMEM, "partition staging buffers");
     SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * (2 * n + 1), h->stream));
     uint64_t *dCompR = dComp + (uint64_t)kTile * tileL[n];
@@ -1549,7 +1607,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
                               (const uint64_t *)dCompR, (const uint32_t *)dCcnt));
         }
         SJBG_CK(h, launch(h, "part_scan", part_scan_win_kernel, dim3(n), dim3(1024), 0, (const WinPlan *)dPlan, dPbL,
-                          dPbR, (const uint32_t *)dCnt, dStart, dCur, (uint32_t)B, dJlist, dJn));
+                          dPbR, (const uint32_t *)dCnt, dStart, dCur, (uint32_t)B, dModels, dJlist, dJn));
         // single-level windows, and compacted windows (their packed light tuples):
         // a local counting sort per tile
         if (any_one || (learned && !enumerate)) {
@@ -1587,7 +1645,7 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         allow_big_smem(bucket_join_enum_kernel, smem);
         SJBG_CK(h, launch(h, "bucket_join_enum", bucket_join_enum_kernel, jgrid, dim3(kJoinThreads), smem,
                           dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, dPlan, dPairs, bits, queue,
-                          (const uint32_t *)dJlist, (const uint32_t *)dJn));
+                          (const JoinItem *)dJlist, (const uint32_t *)dJn));
     } else {
         const uint32_t cap = count_table_cap((uint32_t)target);
         const size_t smem =
@@ -1598,8 +1656,8 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
             jgrid = dim3((uint32_t)std::min<uint64_t>(B, (uint64_t)h->num_sms * std::min<uint32_t>(per_sm, 2u)));
         }
         SJBG_CK(h, launch(h, "bucket_join_count", bucket_join_count_kernel, jgrid, dim3(kJoinThreads), smem,
-                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, cap, queue, (const uint32_t *)dJlist,
-                          (const uint32_t *)dJn, (const WinPlan *)dPlan, dModels));
+                          dPL, dPR, dStart, dCnt, (uint32_t)B, dBwin, acc, cap, queue, (const JoinItem *)dJlist,
+                          (const uint32_t *)dJn));
     }
     return SJBG_OK;
 }
@@ -1735,7 +1793,7 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(uint32_t)) * (cap + 1) + 16;
         allow_big_smem(bucket_join_count_kernel, smem);
         bucket_join_count_kernel<<<P, kJoinThreads, smem, st>>>(pL, pR, start, cnt, P, bwin, rs->acc, cap, nullptr,
-                                                                nullptr, nullptr, nullptr, nullptr);
+                                                                nullptr, nullptr);
         if (int rc = launched("sjbg_lazy_hj_noalloc: bucket_join_count_kernel")) return rc;
     }
     raw_finish_kernel<<<1, 32, 0, st>>>(rs, dOut);
