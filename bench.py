@@ -1070,10 +1070,10 @@ def main():
     e2e_s = sorted(call_s)[len(call_s) // 2]
     e2e_mean_s = sum(call_s) / len(call_s)
     e2e_same = [(r.count, r.prod_checksum) for r in e2e_res] == [(a[0], a[1]) for a in res_learned]
-    # the same windows pushed in batches of 2^20 tuples through the device-resident
-    # ingest ring: copies of window k+1 overlap the join of window k
+    # the same windows pushed in batches of 2^20 tuples (at most a window) through
+    # the device-resident ingest ring: copies of window k+1 overlap the join of window k
     ring = sjbg.Joiner(partitioner=primary_part, **flags_common)
-    RB = 1 << 20
+    RB = min(1 << 20, W)
 
     def ring_pass():
         ring.ring_open(W, 3)
@@ -1154,7 +1154,7 @@ def main():
                 "link_bound_tuples_per_s": max(h2d_gbs, h2d_gbs_two) * 1e9 / 16,
                 "device_ring": {"value": tuples / sorted(ring_s)[len(ring_s) // 2], "unit": "tuples/s",
                                 "outputs_identical": ring_same,
-                                "call": "sjbg_ring_push of pinned batches of 2^20 tuples, sjbg_ring_close"}},
+                                "call": f"sjbg_ring_push of pinned batches of {RB} tuples, sjbg_ring_close"}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,

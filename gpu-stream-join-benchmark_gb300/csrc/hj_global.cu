@@ -51,6 +51,25 @@ __device__ __forceinline__ uint32_t gfind_window(const uint32_t *prefix, uint32_
     return lo;
 }
 
+// 128-bit compare-and-swap of a slot held as two 64-bit words (lo = tag |
+// count << 32, hi = sum): installs want when the slot equals cmp; returns the
+// slot's prior low word (tag and count), which is all the callers test.
+__device__ __forceinline__ unsigned long long gslot_cas(GSlot *s, unsigned long long cmp_lo, unsigned long long cmp_hi,
+                                                        unsigned long long want_lo, unsigned long long want_hi) {
+    unsigned long long lo, hi;
+    asm volatile(
+        "{\n\t.reg .b128 d, b, c;\n\t"
+        "mov.b128 b, {%2, %3};\n\t"
+        "mov.b128 c, {%4, %5};\n\t"
+        "atom.global.cas.b128 d, [%6], b, c;\n\t"
+        "mov.b128 {%0, %1}, d;\n\t}"
+        : "=l"(lo), "=l"(hi)
+        : "l"(cmp_lo), "l"(cmp_hi), "l"(want_lo), "l"(want_hi), "l"(s)
+        : "memory");
+    (void)hi;
+    return lo;
+}
+
 // Slot of `key` in a table of 2^bits slots: claimed when absent (insert) or
 // looked up (insert == false, returns 0xFFFFFFFF when absent).  The table is
 // at most half full, so a probe ends within 2^bits steps.
@@ -74,7 +93,7 @@ __device__ __forceinline__ uint32_t gslot(Slot *t, uint32_t bits, uint32_t key, 
     return 0xFFFFFFFFu;
 }
 
-__global__ void __launch_bounds__(kGThreads)
+__global__ void __launch_bounds__(kGThreads, 4)
 gbuild_count_kernel(const sjbg_tuple *__restrict__ L, const GWin *__restrict__ wins, uint32_t nwin,
                     const uint32_t *__restrict__ tiles, GSlot *__restrict__ table, uint32_t *err) {
     const uint32_t w = gfind_window(tiles, nwin, blockIdx.x);
@@ -90,36 +109,91 @@ gbuild_count_kernel(const sjbg_tuple *__restrict__ L, const GWin *__restrict__ w
         v[k] = i < n ? __ldg(src + 2 * i) : make_uint2(0u, 0u);
     }
     const unsigned full = 0xFFFFFFFFu;
+    const uint32_t C = 1u << wp.bits;
+    // four tuples at a time: their groups, then their slots claimed or found at
+    // once (one round trip for the four, not one per tuple)
+    constexpr int kGroup = 4;
+    static_assert(kGPer % kGroup == 0, "tuples per thread in groups of four");
 #pragma unroll
-    for (int k = 0; k < kGPer; k++) {
-        const bool valid = threadIdx.x + k * kGThreads < n;
-        const uint32_t key = v[k].x;
-        const unsigned long long f = valid ? sjbg_fr(v[k].y) : 0ull;
+    for (int g = 0; g < kGPer; g += kGroup) {
         // lanes with equal keys: the leader adds the group's count and fr-sum
-        const unsigned active = __ballot_sync(full, valid);
-        unsigned grp = __match_any_sync(full, key) & active;
-        if (!valid) grp = 1u << lane_id();
-        const int leader = __ffs(grp) - 1;
-        unsigned long long gsum = f;
-        unsigned multi = __ballot_sync(full, valid && __popc(grp) > 1 && (int)lane_id() == leader);
-        while (multi) {
-            const int ld = __ffs(multi) - 1;
-            multi &= multi - 1;
-            const unsigned m = __shfl_sync(full, grp, ld);
-            const unsigned long long sm = warp_sum_u64(((m >> lane_id()) & 1u) ? f : 0ull);
-            if ((int)lane_id() == ld) gsum = sm;
-        }
-        if (valid && (int)lane_id() == leader) {
-            const uint32_t s = gslot(t, wp.bits, key, true, err);
-            if (s != 0xFFFFFFFFu) {
-                atomicAdd(&t[s].cnt, (uint32_t)__popc(grp));
-                atomicAdd(&t[s].sumf, gsum);
+        unsigned lead = 0;   // bit q: this lane leads tuple g + q's group
+        uint32_t gcnt[kGroup];
+        unsigned long long gsum[kGroup];
+#pragma unroll
+        for (int q = 0; q < kGroup; q++) {
+            const int k = g + q;
+            const bool valid = threadIdx.x + k * kGThreads < n;
+            const uint32_t key = v[k].x;
+            const unsigned long long f = valid ? sjbg_fr(v[k].y) : 0ull;
+            const unsigned active = __ballot_sync(full, valid);
+            unsigned grp = __match_any_sync(full, key) & active;
+            if (!valid) grp = 1u << lane_id();
+            const int leader = __ffs(grp) - 1;
+            gsum[q] = f;
+            gcnt[q] = __popc(grp);
+            unsigned multi = __ballot_sync(full, valid && __popc(grp) > 1 && (int)lane_id() == leader);
+            while (multi) {
+                const int ld = __ffs(multi) - 1;
+                multi &= multi - 1;
+                const unsigned m = __shfl_sync(full, grp, ld);
+                const unsigned long long sm = warp_sum_u64(((m >> lane_id()) & 1u) ? f : 0ull);
+                if ((int)lane_id() == ld) gsum[q] = sm;
             }
+            if (valid && (int)lane_id() == leader) lead |= 1u << q;
+        }
+        // A 128-bit compare-and-swap of an all-zero slot installs {tag, count,
+        // sum} whole, so a key new to the table costs one atomic; otherwise it
+        // returns the slot, and a slot holding the key gets the count and sum
+        // added (a taken slot's count is never 0)
+        uint32_t slot[kGroup], got[kGroup];   // got: the tag found in the slot
+#pragma unroll
+        for (int q = 0; q < kGroup; q++) {
+            const uint32_t key = v[g + q].x;
+            slot[q] = C;
+            got[q] = 0u;
+            if (((lead >> q) & 1u) && key != 0xFFFFFFFFu) {
+                slot[q] = slot_hash(key, wp.bits);
+                const unsigned long long old = gslot_cas(&t[slot[q]], 0ull, 0ull,
+                                                         (unsigned long long)(~key) | ((unsigned long long)gcnt[q] << 32),
+                                                         gsum[q]);
+                got[q] = (uint32_t)old;
+                if ((old >> 32) == 0ull) lead &= ~(1u << q);   // installed: nothing left to add
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kGroup; q++) {
+            if (!((lead >> q) & 1u)) continue;
+            const uint32_t key = v[g + q].x;
+            if (key != 0xFFFFFFFFu) {
+                const uint32_t tag = ~key;
+                uint32_t p = 1;
+                bool installed = false;
+                while (got[q] != tag && p < C) {
+                    slot[q] = (slot[q] + 1) & (C - 1);
+                    const unsigned long long old = gslot_cas(&t[slot[q]], 0ull, 0ull,
+                                                             (unsigned long long)tag | ((unsigned long long)gcnt[q] << 32),
+                                                             gsum[q]);
+                    if ((old >> 32) == 0ull) {
+                        installed = true;
+                        break;
+                    }
+                    got[q] = (uint32_t)old;
+                    p++;
+                }
+                if (installed) continue;
+                if (got[q] != tag) {   // the whole table is taken: cannot happen at load <= 1/2
+                    atomicOr(err, kErrTableFull);
+                    continue;
+                }
+            }
+            atomicAdd(&t[slot[q]].cnt, gcnt[q]);
+            atomicAdd(&t[slot[q]].sumf, gsum[q]);
         }
     }
 }
 
-__global__ void __launch_bounds__(kGThreads)
+__global__ void __launch_bounds__(kGThreads, 4)
 gprobe_count_kernel(const sjbg_tuple *__restrict__ R, const GWin *__restrict__ wins, uint32_t nwin,
                     const uint32_t *__restrict__ tiles, const GSlot *__restrict__ table, WinAcc *__restrict__ acc) {
     const uint32_t w = gfind_window(tiles, nwin, blockIdx.x);
@@ -136,28 +210,42 @@ gprobe_count_kernel(const sjbg_tuple *__restrict__ R, const GWin *__restrict__ w
         v[k] = i < n ? __ldg(src + 2 * i) : make_uint2(0u, 0u);
     }
     unsigned long long count = 0, prod = 0;
+    // every tuple's home slot is read at once (one 16-byte load: tag, count
+    // and sum together), then collisions walk on
+    GSlot e[kGPer];
+    uint32_t slot[kGPer];
+#pragma unroll
+    for (int k = 0; k < kGPer; k++) {
+        const uint32_t key = v[k].x;
+        slot[k] = key == 0xFFFFFFFFu ? C : slot_hash(key, wp.bits);
+        if (threadIdx.x + k * kGThreads < n) {
+            const uint4 q = __ldg(reinterpret_cast<const uint4 *>(&t[slot[k]]));
+            e[k].tag = q.x;
+            e[k].cnt = q.y;
+            e[k].sumf = ((unsigned long long)q.w << 32) | q.z;
+        } else {
+            e[k].tag = 0u;
+            e[k].cnt = 0u;
+            e[k].sumf = 0ull;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < kGPer; k++) {
         if (threadIdx.x + k * kGThreads >= n) continue;
         const uint32_t key = v[k].x;
-        uint32_t s;
-        if (key == 0xFFFFFFFFu) {
-            s = C;
-        } else {
+        if (key != 0xFFFFFFFFu) {   // (slot C of key 0xFFFFFFFF needs no tag test)
             const uint32_t tag = ~key;
-            s = slot_hash(key, wp.bits);
-            for (uint32_t p = 0; p < C; p++) {
-                const uint32_t cur = __ldg(&t[s].tag);
-                if (cur == tag) break;
-                if (cur == 0u) { s = 0xFFFFFFFFu; break; }
-                s = (s + 1) & (C - 1);
+            for (uint32_t p = 1; e[k].tag != tag && e[k].tag != 0u && p < C; p++) {
+                slot[k] = (slot[k] + 1) & (C - 1);
+                const uint4 q = __ldg(reinterpret_cast<const uint4 *>(&t[slot[k]]));
+                e[k].tag = q.x;
+                e[k].cnt = q.y;
+                e[k].sumf = ((unsigned long long)q.w << 32) | q.z;
             }
+            if (e[k].tag != tag) continue;
         }
-        if (s != 0xFFFFFFFFu) {
-            const GSlot e = t[s];
-            count += e.cnt;
-            prod += e.sumf * sjbg_gs(v[k].y);
-        }
+        count += e[k].cnt;
+        prod += e[k].sumf * sjbg_gs(v[k].y);
     }
     flush_acc(&acc[w], count, 0, prod);
 }
