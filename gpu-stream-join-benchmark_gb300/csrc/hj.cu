@@ -744,7 +744,53 @@ __device__ __forceinline__ void scatter_tile(const WorkItem it, const TileIn in,
     }
 }
 
-__global__ void __launch_bounds__(kPartThreads, 2)
+// scatter_tile for a radix window (no model, no heavy keys, not compacted):
+// a tuple's bucket is key & mask, so the staged word carries it and no bucket
+// array is kept; the write-out reads one per-bucket delta (global base minus
+// local offset) per tuple.
+__device__ __forceinline__ void scatter_tile_radix(const WorkItem it, const TileIn in, uint64_t (&e)[kScatterPer],
+                                                   const TileIn *next, const WinPlan *__restrict__ wins,
+                                                   uint32_t *__restrict__ cursor, uint32_t B,
+                                                   uint64_t *__restrict__ outL, uint64_t *__restrict__ outR) {
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    __shared__ uint32_t warp_tot[32];
+    const WinPlan wp = wins[it.w];
+    const uint32_t mask = (1u << wp.log2_buckets) - 1u, P = mask + 1u;
+    const uint32_t n = in.n;
+    uint64_t *stage = reinterpret_cast<uint64_t *>(smem_raw);   // kTile
+    uint32_t *lcnt = reinterpret_cast<uint32_t *>(stage + kTile);  // P
+    uint32_t *delta = lcnt + P;                                  // P
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) lcnt[i] = 0;
+    SJBG_BARRIER();
+    uint32_t rk[kScatterPer];
+#pragma unroll
+    for (int k = 0; k < kScatterPer; k++)
+        if (threadIdx.x + k * kPartThreads < n) rk[k] = atomicAdd(&lcnt[(uint32_t)e[k] & mask], 1u);
+    SJBG_BARRIER();
+    if (next && threadIdx.x == 0) l2_prefetch_bulk(next->p, (size_t)next->n * (next->packed ? 8u : 16u));
+    // reserve one global range per non-empty bucket
+    uint32_t *gcur = cursor + (it.right ? B : 0) + wp.bucket_base;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        const uint32_t c = lcnt[i];
+        delta[i] = c ? atomicAdd(&gcur[i], c) : 0;
+    }
+    block_scan_smem(lcnt, P, warp_tot);   // lcnt -> local offsets (ends with a barrier)
+#pragma unroll
+    for (int k = 0; k < kScatterPer; k++)
+        if (threadIdx.x + k * kPartThreads < n) stage[lcnt[(uint32_t)e[k] & mask] + rk[k]] = e[k];
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) delta[i] -= lcnt[i];   // (mod 2^32)
+    if (next) tile_load(*next, e);
+    SJBG_BARRIER();
+    uint64_t *out = it.right ? outR : outL;
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const uint64_t x = stage[j];
+        out[delta[(uint32_t)x & mask] + j] = x;
+    }
+}
+
+// kRadixOnly: no window of the call has a model (compiled without the general path).
+template <bool kRadixOnly>
+__global__ void __launch_bounds__(kPartThreads, kRadixOnly ? 3 : 2)
 part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restrict__ R, const WinPlan *__restrict__ wins,
                     uint32_t nwin, const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
                     const uint32_t *__restrict__ workL, const uint32_t *__restrict__ workR,
@@ -770,7 +816,10 @@ part_scatter_kernel(const sjbg_tuple *__restrict__ L, const sjbg_tuple *__restri
             nit = work_item(workL, workR, nwin, nb);
             nin = tile_input(nit, L, R, wins, tileL, tileR, models, compL, compR, ccnt);
         }
-        scatter_tile(it, in, e, nb < items ? &nin : nullptr, wins, cursor, B, outL, outR, models);
+        if (kRadixOnly || (!in.packed && !model_of(wins[it.w], models)))
+            scatter_tile_radix(it, in, e, nb < items ? &nin : nullptr, wins, cursor, B, outL, outR);
+        else
+            scatter_tile(it, in, e, nb < items ? &nin : nullptr, wins, cursor, B, outL, outR, models);
         it = nit;
         in = nin;
     }
@@ -1612,10 +1661,12 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
         // a local counting sort per tile
         if (any_one || (learned && !enumerate)) {
             const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * maxP;
-            allow_big_smem(part_scatter_kernel, scatterSmem);
+            // without a learned partitioner every window is radix-partitioned
+            auto scatter = learned ? part_scatter_kernel<false> : part_scatter_kernel<true>;
+            allow_big_smem(scatter, scatterSmem);
             const uint32_t sgrid = std::min<uint32_t>(tiles, 3u * 4u * (uint32_t)h->num_sms);
             const uint32_t *wS = dWork + 2 * kWorkScatter * (n + 1);
-            SJBG_CK(h, launch(h, "part_scatter", part_scatter_kernel, dim3(sgrid), dim3(kPartThreads), scatterSmem,
+            SJBG_CK(h, launch(h, "part_scatter", scatter, dim3(sgrid), dim3(kPartThreads), scatterSmem,
                               dL, dR, dPlan, n, dTileL, dTileR, wS, wS + (n + 1), dCur, (uint32_t)B, dPL, dPR,
                               dModels, (const uint64_t *)dComp, (const uint64_t *)dCompR, (const uint32_t *)dCcnt));
         }
@@ -1783,9 +1834,9 @@ int hj_count_window_raw(const sjbg_tuple *dL, uint64_t nL, const sjbg_tuple *dR,
         part_scan_kernel<<<1, 1024, 0, st>>>(cnt, start, cur, P);
         if (int rc = launched("sjbg_lazy_hj_noalloc: part_scan_kernel")) return rc;
         const size_t scatterSmem = kTile * (sizeof(uint64_t) + sizeof(uint16_t)) + 2 * sizeof(uint32_t) * P;
-        allow_big_smem(part_scatter_kernel, scatterSmem);
+        allow_big_smem(part_scatter_kernel<true>, scatterSmem);
         // a single-level radix window: the scatter work is every tile
-        part_scatter_kernel<<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, tl, tl + 2,
+        part_scatter_kernel<true><<<tL + tR, kPartThreads, scatterSmem, st>>>(dL, dR, &rs->plan, 1, tl, tl + 2, tl, tl + 2,
                                                                           cur, P, pL, pR, nullptr, nullptr, nullptr,
                                                                           nullptr);
         if (int rc = launched("sjbg_lazy_hj_noalloc: part_scatter_kernel")) return rc;
