@@ -612,10 +612,13 @@ def suite_eager_run(args, sjbg, torch, dev, peak, sm_mhz, algo, W, D, n_batches)
     if algo == "NLJ" and top:
         # compare-bound: every (left batch, right batch) pair of a window compares B x B keys
         compares = sum(len(lb) * len(rb) for lb, rb in eager_windows(n_batches, B, W)) * B * B
-        peak_cmp = 152 * 128 * (sm_mhz or 2070.0) * 1e6   # SMs x int32 lanes per SM x clock
+        # an integer compare issues to the SM's ALU pipe, which takes 64 lanes per clock
+        # (ncu: sm__inst_executed_pipe_alu at 82 % of peak with 1.64 ALU warp
+        # instructions per clock, profiles/eager_nlj_blocks_eager_nlj_65536.md)
+        peak_cmp = 152 * 64 * (sm_mhz or 2070.0) * 1e6   # SMs x ALU lanes per SM x clock
         achieved = compares / (top["launch_ms"] * top["launches_per_step"] * 1e-3)
         top.update(bound="int-compare", achieved_compares_per_s=achieved, peak_compares_per_s=peak_cmp,
-                   frac=achieved / peak_cmp, peak_kind="152 SMs x 128 int32 lanes x median SM clock")
+                   frac=achieved / peak_cmp, peak_kind="152 SMs x 64 ALU lanes x median SM clock")
     j.close()
     prof.close()
     return {"value": 2 * n / (ms * 1e-3), "unit": "tuples/s", "ms_per_step": ms,

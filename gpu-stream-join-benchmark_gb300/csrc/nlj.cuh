@@ -13,55 +13,166 @@ constexpr uint32_t kChunk = 2048;                // right tuples per shared-memo
 constexpr uint32_t kRSplit = 16384;              // right tuples per CTA
 constexpr uint32_t kVote = 64;                   // right keys between warp votes
 
-// Whether any of the thread's 8 left keys equals any of 4 right keys: the 32
-// compares as PTX setp.eq with an OR into the predicate (one instruction per
-// compare), in four independent chains (one per right key) merged at the end.
-static_assert(kLReg == 8, "any_equal_8x4 compares 8 left keys");
-__device__ __forceinline__ uint32_t any_equal_8x4(const uint32_t (&l)[kLReg], const uint4 k) {
-    uint32_t hit;
-    asm("{\n\t"
-        ".reg .pred p0, p1, p2, p3;\n\t"
-        "setp.eq.u32 p0, %1, %9;\n\t"
-        "setp.eq.u32 p1, %1, %10;\n\t"
-        "setp.eq.u32 p2, %1, %11;\n\t"
-        "setp.eq.u32 p3, %1, %12;\n\t"
-        "setp.eq.or.u32 p0, %2, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %2, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %2, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %2, %12, p3;\n\t"
-        "setp.eq.or.u32 p0, %3, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %3, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %3, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %3, %12, p3;\n\t"
-        "setp.eq.or.u32 p0, %4, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %4, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %4, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %4, %12, p3;\n\t"
-        "setp.eq.or.u32 p0, %5, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %5, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %5, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %5, %12, p3;\n\t"
-        "setp.eq.or.u32 p0, %6, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %6, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %6, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %6, %12, p3;\n\t"
-        "setp.eq.or.u32 p0, %7, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %7, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %7, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %7, %12, p3;\n\t"
-        "setp.eq.or.u32 p0, %8, %9, p0;\n\t"
-        "setp.eq.or.u32 p1, %8, %10, p1;\n\t"
-        "setp.eq.or.u32 p2, %8, %11, p2;\n\t"
-        "setp.eq.or.u32 p3, %8, %12, p3;\n\t"
+// Which of 4 quads of right keys (16 keys at shared-memory address `rk`,
+// 16-byte aligned) hold a key equal to one of the thread's 8 left keys: bit q
+// of the result for quad q.  The 128 compares are PTX setp.eq with an OR into
+// the predicate, one instruction per compare, in eight independent chains (two
+// per quad: left keys 0-3 and 4-7), so the integer pipe sees about one
+// instruction per compare; seven more form the mask.
+static_assert(kLReg == 8, "quads_equal_8x16 compares 8 left keys");
+__device__ __forceinline__ uint32_t quads_equal_8x16(const uint32_t (&l)[kLReg], uint32_t rk) {
+    uint32_t m;
+    asm volatile("{\n\t"
+        ".reg .b32 a<16>, t;\n\t"
+        ".reg .pred p<8>;\n\t"
+        "ld.shared.v4.u32 {a0, a1, a2, a3}, [%9+0];\n\t"
+        "ld.shared.v4.u32 {a4, a5, a6, a7}, [%9+16];\n\t"
+        "ld.shared.v4.u32 {a8, a9, a10, a11}, [%9+32];\n\t"
+        "ld.shared.v4.u32 {a12, a13, a14, a15}, [%9+48];\n\t"
+        "setp.eq.u32 p0, %1, a0;\n\t"
+        "setp.eq.u32 p1, %5, a0;\n\t"
+        "setp.eq.u32 p2, %1, a4;\n\t"
+        "setp.eq.u32 p3, %5, a4;\n\t"
+        "setp.eq.u32 p4, %1, a8;\n\t"
+        "setp.eq.u32 p5, %5, a8;\n\t"
+        "setp.eq.u32 p6, %1, a12;\n\t"
+        "setp.eq.u32 p7, %5, a12;\n\t"
+        "setp.eq.or.u32 p0, %2, a0, p0;\n\t"
+        "setp.eq.or.u32 p1, %6, a0, p1;\n\t"
+        "setp.eq.or.u32 p2, %2, a4, p2;\n\t"
+        "setp.eq.or.u32 p3, %6, a4, p3;\n\t"
+        "setp.eq.or.u32 p4, %2, a8, p4;\n\t"
+        "setp.eq.or.u32 p5, %6, a8, p5;\n\t"
+        "setp.eq.or.u32 p6, %2, a12, p6;\n\t"
+        "setp.eq.or.u32 p7, %6, a12, p7;\n\t"
+        "setp.eq.or.u32 p0, %3, a0, p0;\n\t"
+        "setp.eq.or.u32 p1, %7, a0, p1;\n\t"
+        "setp.eq.or.u32 p2, %3, a4, p2;\n\t"
+        "setp.eq.or.u32 p3, %7, a4, p3;\n\t"
+        "setp.eq.or.u32 p4, %3, a8, p4;\n\t"
+        "setp.eq.or.u32 p5, %7, a8, p5;\n\t"
+        "setp.eq.or.u32 p6, %3, a12, p6;\n\t"
+        "setp.eq.or.u32 p7, %7, a12, p7;\n\t"
+        "setp.eq.or.u32 p0, %4, a0, p0;\n\t"
+        "setp.eq.or.u32 p1, %8, a0, p1;\n\t"
+        "setp.eq.or.u32 p2, %4, a4, p2;\n\t"
+        "setp.eq.or.u32 p3, %8, a4, p3;\n\t"
+        "setp.eq.or.u32 p4, %4, a8, p4;\n\t"
+        "setp.eq.or.u32 p5, %8, a8, p5;\n\t"
+        "setp.eq.or.u32 p6, %4, a12, p6;\n\t"
+        "setp.eq.or.u32 p7, %8, a12, p7;\n\t"
+        "setp.eq.or.u32 p0, %1, a1, p0;\n\t"
+        "setp.eq.or.u32 p1, %5, a1, p1;\n\t"
+        "setp.eq.or.u32 p2, %1, a5, p2;\n\t"
+        "setp.eq.or.u32 p3, %5, a5, p3;\n\t"
+        "setp.eq.or.u32 p4, %1, a9, p4;\n\t"
+        "setp.eq.or.u32 p5, %5, a9, p5;\n\t"
+        "setp.eq.or.u32 p6, %1, a13, p6;\n\t"
+        "setp.eq.or.u32 p7, %5, a13, p7;\n\t"
+        "setp.eq.or.u32 p0, %2, a1, p0;\n\t"
+        "setp.eq.or.u32 p1, %6, a1, p1;\n\t"
+        "setp.eq.or.u32 p2, %2, a5, p2;\n\t"
+        "setp.eq.or.u32 p3, %6, a5, p3;\n\t"
+        "setp.eq.or.u32 p4, %2, a9, p4;\n\t"
+        "setp.eq.or.u32 p5, %6, a9, p5;\n\t"
+        "setp.eq.or.u32 p6, %2, a13, p6;\n\t"
+        "setp.eq.or.u32 p7, %6, a13, p7;\n\t"
+        "setp.eq.or.u32 p0, %3, a1, p0;\n\t"
+        "setp.eq.or.u32 p1, %7, a1, p1;\n\t"
+        "setp.eq.or.u32 p2, %3, a5, p2;\n\t"
+        "setp.eq.or.u32 p3, %7, a5, p3;\n\t"
+        "setp.eq.or.u32 p4, %3, a9, p4;\n\t"
+        "setp.eq.or.u32 p5, %7, a9, p5;\n\t"
+        "setp.eq.or.u32 p6, %3, a13, p6;\n\t"
+        "setp.eq.or.u32 p7, %7, a13, p7;\n\t"
+        "setp.eq.or.u32 p0, %4, a1, p0;\n\t"
+        "setp.eq.or.u32 p1, %8, a1, p1;\n\t"
+        "setp.eq.or.u32 p2, %4, a5, p2;\n\t"
+        "setp.eq.or.u32 p3, %8, a5, p3;\n\t"
+        "setp.eq.or.u32 p4, %4, a9, p4;\n\t"
+        "setp.eq.or.u32 p5, %8, a9, p5;\n\t"
+        "setp.eq.or.u32 p6, %4, a13, p6;\n\t"
+        "setp.eq.or.u32 p7, %8, a13, p7;\n\t"
+        "setp.eq.or.u32 p0, %1, a2, p0;\n\t"
+        "setp.eq.or.u32 p1, %5, a2, p1;\n\t"
+        "setp.eq.or.u32 p2, %1, a6, p2;\n\t"
+        "setp.eq.or.u32 p3, %5, a6, p3;\n\t"
+        "setp.eq.or.u32 p4, %1, a10, p4;\n\t"
+        "setp.eq.or.u32 p5, %5, a10, p5;\n\t"
+        "setp.eq.or.u32 p6, %1, a14, p6;\n\t"
+        "setp.eq.or.u32 p7, %5, a14, p7;\n\t"
+        "setp.eq.or.u32 p0, %2, a2, p0;\n\t"
+        "setp.eq.or.u32 p1, %6, a2, p1;\n\t"
+        "setp.eq.or.u32 p2, %2, a6, p2;\n\t"
+        "setp.eq.or.u32 p3, %6, a6, p3;\n\t"
+        "setp.eq.or.u32 p4, %2, a10, p4;\n\t"
+        "setp.eq.or.u32 p5, %6, a10, p5;\n\t"
+        "setp.eq.or.u32 p6, %2, a14, p6;\n\t"
+        "setp.eq.or.u32 p7, %6, a14, p7;\n\t"
+        "setp.eq.or.u32 p0, %3, a2, p0;\n\t"
+        "setp.eq.or.u32 p1, %7, a2, p1;\n\t"
+        "setp.eq.or.u32 p2, %3, a6, p2;\n\t"
+        "setp.eq.or.u32 p3, %7, a6, p3;\n\t"
+        "setp.eq.or.u32 p4, %3, a10, p4;\n\t"
+        "setp.eq.or.u32 p5, %7, a10, p5;\n\t"
+        "setp.eq.or.u32 p6, %3, a14, p6;\n\t"
+        "setp.eq.or.u32 p7, %7, a14, p7;\n\t"
+        "setp.eq.or.u32 p0, %4, a2, p0;\n\t"
+        "setp.eq.or.u32 p1, %8, a2, p1;\n\t"
+        "setp.eq.or.u32 p2, %4, a6, p2;\n\t"
+        "setp.eq.or.u32 p3, %8, a6, p3;\n\t"
+        "setp.eq.or.u32 p4, %4, a10, p4;\n\t"
+        "setp.eq.or.u32 p5, %8, a10, p5;\n\t"
+        "setp.eq.or.u32 p6, %4, a14, p6;\n\t"
+        "setp.eq.or.u32 p7, %8, a14, p7;\n\t"
+        "setp.eq.or.u32 p0, %1, a3, p0;\n\t"
+        "setp.eq.or.u32 p1, %5, a3, p1;\n\t"
+        "setp.eq.or.u32 p2, %1, a7, p2;\n\t"
+        "setp.eq.or.u32 p3, %5, a7, p3;\n\t"
+        "setp.eq.or.u32 p4, %1, a11, p4;\n\t"
+        "setp.eq.or.u32 p5, %5, a11, p5;\n\t"
+        "setp.eq.or.u32 p6, %1, a15, p6;\n\t"
+        "setp.eq.or.u32 p7, %5, a15, p7;\n\t"
+        "setp.eq.or.u32 p0, %2, a3, p0;\n\t"
+        "setp.eq.or.u32 p1, %6, a3, p1;\n\t"
+        "setp.eq.or.u32 p2, %2, a7, p2;\n\t"
+        "setp.eq.or.u32 p3, %6, a7, p3;\n\t"
+        "setp.eq.or.u32 p4, %2, a11, p4;\n\t"
+        "setp.eq.or.u32 p5, %6, a11, p5;\n\t"
+        "setp.eq.or.u32 p6, %2, a15, p6;\n\t"
+        "setp.eq.or.u32 p7, %6, a15, p7;\n\t"
+        "setp.eq.or.u32 p0, %3, a3, p0;\n\t"
+        "setp.eq.or.u32 p1, %7, a3, p1;\n\t"
+        "setp.eq.or.u32 p2, %3, a7, p2;\n\t"
+        "setp.eq.or.u32 p3, %7, a7, p3;\n\t"
+        "setp.eq.or.u32 p4, %3, a11, p4;\n\t"
+        "setp.eq.or.u32 p5, %7, a11, p5;\n\t"
+        "setp.eq.or.u32 p6, %3, a15, p6;\n\t"
+        "setp.eq.or.u32 p7, %7, a15, p7;\n\t"
+        "setp.eq.or.u32 p0, %4, a3, p0;\n\t"
+        "setp.eq.or.u32 p1, %8, a3, p1;\n\t"
+        "setp.eq.or.u32 p2, %4, a7, p2;\n\t"
+        "setp.eq.or.u32 p3, %8, a7, p3;\n\t"
+        "setp.eq.or.u32 p4, %4, a11, p4;\n\t"
+        "setp.eq.or.u32 p5, %8, a11, p5;\n\t"
+        "setp.eq.or.u32 p6, %4, a15, p6;\n\t"
+        "setp.eq.or.u32 p7, %8, a15, p7;\n\t"
         "or.pred p0, p0, p1;\n\t"
         "or.pred p2, p2, p3;\n\t"
-        "or.pred p0, p0, p2;\n\t"
+        "or.pred p4, p4, p5;\n\t"
+        "or.pred p6, p6, p7;\n\t"
         "selp.u32 %0, 1, 0, p0;\n\t"
+        "selp.u32 t, 2, 0, p2;\n\t"
+        "or.b32 %0, %0, t;\n\t"
+        "selp.u32 t, 4, 0, p4;\n\t"
+        "or.b32 %0, %0, t;\n\t"
+        "selp.u32 t, 8, 0, p6;\n\t"
+        "or.b32 %0, %0, t;\n\t"
         "}"
-        : "=r"(hit)
-        : "r"(l[0]), "r"(l[1]), "r"(l[2]), "r"(l[3]), "r"(l[4]), "r"(l[5]), "r"(l[6]), "r"(l[7]), "r"(k.x),
-          "r"(k.y), "r"(k.z), "r"(k.w));
-    return hit;
+        : "=r"(m)
+        : "r"(l[0]), "r"(l[1]), "r"(l[2]), "r"(l[3]), "r"(l[4]), "r"(l[5]), "r"(l[6]), "r"(l[7]), "r"(rk)
+        : "memory");
+    return m;
 }
 
 // Load of a (key, val) pair.  Kernels whose inputs do not change while they
@@ -118,27 +229,28 @@ __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uin
             }
         }
         SJBG_BARRIER();
-        const uint4 *rk4 = reinterpret_cast<const uint4 *>(rkeys);
+        const uint32_t rbase = (uint32_t)__cvta_generic_to_shared(rkeys);
         for (uint32_t r = 0; r < mpad; r += kVote) {
-            bool p = false;
-#pragma unroll 4
-            for (uint32_t q = 0; q < kVote / 4; q++) {
-                const uint4 k4 = rk4[(r >> 2) + q];
-                p |= any_equal_8x4(lk, k4) != 0u;
-            }
-            if (!__any_sync(0xFFFFFFFFu, p)) continue;
-            // exact path for this group of kVote right keys (warp-uniform)
-            const uint32_t qe = min(r + kVote, m);
-            uint32_t mine = 0;
-            for (uint32_t q = r; q < qe; q++) {
-                const uint32_t k = rkeys[q];
+            // bit q: right keys r + 4q .. r + 4q + 3 hold a key equal to one of this lane's
+            uint32_t hits = 0;
 #pragma unroll
-                for (int a = 0; a < kLReg; a++) {
-                    if (((lvalid >> a) & 1u) && lk[a] == k) {
-                        const uint32_t sv = rvals[q];
-                        mine++;
-                        prod += sjbg_fr(lv[a]) * sjbg_gs(sv);
-                        if (kEnum) xr ^= sjbg_pair_hash(lv[a], sv);
+            for (uint32_t b = 0; b < kVote / 16; b++) hits |= quads_equal_8x16(lk, rbase + 4u * (r + 16u * b)) << (4u * b);
+            if (!__any_sync(0xFFFFFFFFu, hits != 0u)) continue;
+            // exact path (warp-uniform) over the quads that some lane matched
+            const uint32_t quads = __reduce_or_sync(0xFFFFFFFFu, hits);
+            uint32_t mine = 0;
+            for (uint32_t qs = quads; qs; qs &= qs - 1) {
+                const uint32_t q0 = r + 4u * (uint32_t)(__ffs(qs) - 1), qe = min(q0 + 4u, m);
+                for (uint32_t q = q0; q < qe; q++) {
+                    const uint32_t k = rkeys[q];
+#pragma unroll
+                    for (int a = 0; a < kLReg; a++) {
+                        if (((lvalid >> a) & 1u) && lk[a] == k) {
+                            const uint32_t sv = rvals[q];
+                            mine++;
+                            prod += sjbg_fr(lv[a]) * sjbg_gs(sv);
+                            if (kEnum) xr ^= sjbg_pair_hash(lv[a], sv);
+                        }
                     }
                 }
             }
@@ -149,13 +261,16 @@ __device__ __forceinline__ void nlj_block(const sjbg_tuple *__restrict__ Lw, uin
                 unsigned long long base = 0;
                 if (lane_id() == 0 && tot) base = atomicAdd(&acc->npairs, (unsigned long long)tot);
                 base = __shfl_sync(0xFFFFFFFFu, base, 0) + ex;
-                for (uint32_t q = r; q < qe && mine; q++) {
-                    const uint32_t k = rkeys[q];
+                for (uint32_t qs = quads; qs && mine; qs &= qs - 1) {
+                    const uint32_t q0 = r + 4u * (uint32_t)(__ffs(qs) - 1), qe = min(q0 + 4u, m);
+                    for (uint32_t q = q0; q < qe; q++) {
+                        const uint32_t k = rkeys[q];
 #pragma unroll
-                    for (int a = 0; a < kLReg; a++) {
-                        if (((lvalid >> a) & 1u) && lk[a] == k) {
-                            if (base < pcap) pout[base] = sjbg_pair{lv[a], rvals[q]};
-                            base++;
+                        for (int a = 0; a < kLReg; a++) {
+                            if (((lvalid >> a) & 1u) && lk[a] == k) {
+                                if (base < pcap) pout[base] = sjbg_pair{lv[a], rvals[q]};
+                                base++;
+                            }
                         }
                     }
                 }
