@@ -1146,7 +1146,12 @@ constexpr uint32_t kDirectPasses = 2;
 // Larger buckets (a radix window's hot keys) keep the hash table: every extra
 // pass and the table reset re-read the bucket, which one CTA would do serially.
 constexpr uint32_t kDirectMaxRun = 16384;
-constexpr size_t kDirectBytes = (sizeof(unsigned long long) + sizeof(uint32_t)) * kDirectMax;
+// A left run of at most kDirectSave tuples keeps each tuple's table index (16
+// bits, 0xFFFF outside the pass's range) in shared memory during the build, so
+// the table is reset from there instead of from a second read of the run.
+constexpr uint32_t kDirectSave = 4096;
+constexpr size_t kDirectBytes =
+    (sizeof(unsigned long long) + sizeof(uint32_t)) * kDirectMax + sizeof(uint16_t) * kDirectSave;
 
 // `clean`: the leading table entries known to be zero (CTA-uniform); a direct
 // bucket leaves the table zero again, a hash-table bucket does not.  Returns
@@ -1160,6 +1165,8 @@ __device__ __forceinline__ bool join_count_direct(const JoinItem &ji, const uint
     if (nR == 0 || nS == 0) return true;
     unsigned long long *dsum = reinterpret_cast<unsigned long long *>(smem_raw);
     uint32_t *dcnt = reinterpret_cast<uint32_t *>(dsum + kDirectMax);
+    uint16_t *dsave = reinterpret_cast<uint16_t *>(dcnt + kDirectMax);   // kDirectSave indices
+    const bool save = nR <= kDirectSave;
     const uint64_t *Rb = partL + ji.sR;
     const uint64_t *Sb = partR + ji.sS;
     for (uint32_t i = clean + threadIdx.x; i < kDirectMax; i += blockDim.x) {
@@ -1185,10 +1192,12 @@ __device__ __forceinline__ bool join_count_direct(const JoinItem &ji, const uint
             }
 #pragma unroll
             for (int k = 0; k < kJoinPer; k++) {
-                if (base + k * blockDim.x + threadIdx.x < nR) {
+                const uint32_t i = base + k * blockDim.x + threadIdx.x;
+                if (i < nR) {
                     const uint32_t idx = (uint32_t)e[k] >> lg;
                     tmax = max(tmax, idx);
                     const uint32_t d = idx - lo;   // wraps for indices below the range
+                    if (save) dsave[i] = d < kDirectMax ? (uint16_t)d : (uint16_t)0xFFFFu;
                     if (d < kDirectMax) {
                         atomicAdd(&dcnt[d], 1u);
                         ct_add_sum(&dsum[d], sjbg_fr((uint32_t)(e[k] >> 32)));
@@ -1236,9 +1245,10 @@ __device__ __forceinline__ bool join_count_direct(const JoinItem &ji, const uint
             }
         }
         SJBG_BARRIER();
-        // leave the table zero: the range's build entries (the left run again, from L2)
+        // leave the table zero: the range's build entries (their saved indices,
+        // or for a longer run the run again, from L2)
         for (uint32_t i = threadIdx.x; i < nR; i += blockDim.x) {
-            const uint32_t d = ((uint32_t)Rb[i] >> lg) - lo;
+            const uint32_t d = save ? (uint32_t)dsave[i] : ((uint32_t)Rb[i] >> lg) - lo;
             if (d < kDirectMax) {
                 dcnt[d] = 0;
                 dsum[d] = 0;
