@@ -842,18 +842,42 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-constexpr size_t kFineSmem = kFineChunk * (2 * sizeof(uint64_t) + sizeof(uint8_t));
+// Up to kFineGather tuples of an item are gathered at once (all of a typical
+// item's runs, one memory latency), then sorted in chunks of kFineChunk.
+// (Measured: prefetching the next item's runs into L2 from here made the pass
+// slower - reading that item's rows held a warp past the gather.)
+constexpr uint32_t kFineGather = 2 * kFineChunk;
+constexpr size_t kFineSmem = kFineGather * sizeof(uint64_t) + kFineChunk * sizeof(uint8_t);
 
-__device__ __forceinline__ void fine_item(const WorkItem it, const WinPlan *__restrict__ wins, uint32_t nwin,
-                                          const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR,
-                                          uint32_t *__restrict__ cursor, uint32_t B, uint64_t *__restrict__ outL,
-                                          uint64_t *__restrict__ outR, const LearnedModel *__restrict__ models,
-                                          const uint64_t *__restrict__ srcL, const uint64_t *__restrict__ srcR,
-                                          const uint32_t *__restrict__ rows) {
+// An item's coarse partition c and its group of tiles [t0, t0 + G).
+struct FineRuns {
+    uint32_t c, t0, G;
+};
+__device__ __forceinline__ FineRuns fine_runs(const WorkItem it, const WinPlan *__restrict__ wins,
+                                              const uint32_t *__restrict__ tileL, const uint32_t *__restrict__ tileR) {
+    const uint32_t *tp = it.right ? tileR : tileL;
+    const uint32_t w = it.w;
+    const uint32_t ntw = tp[w + 1] - tp[w];
+    const uint32_t ngroups = (ntw + kGroupTiles - 1) / kGroupTiles;
+    FineRuns f;
+    f.c = it.local / ngroups;
+    const uint32_t g = it.local % ngroups;
+    f.t0 = g * kGroupTiles;
+    f.G = min(kGroupTiles, ntw - f.t0);
+    return f;
+}
+
+__device__ __forceinline__ void fine_item(const WorkItem it, const WinPlan *__restrict__ wins,
+                                          uint32_t nwin, const uint32_t *__restrict__ tileL,
+                                          const uint32_t *__restrict__ tileR, uint32_t *__restrict__ cursor, uint32_t B,
+                                          uint64_t *__restrict__ outL, uint64_t *__restrict__ outR,
+                                          const LearnedModel *__restrict__ models, const uint64_t *__restrict__ srcL,
+                                          const uint64_t *__restrict__ srcR, const uint32_t *__restrict__ rows) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    uint64_t *tmp = reinterpret_cast<uint64_t *>(smem_raw);       // kFineChunk gathered tuples
-    uint64_t *stage = tmp + kFineChunk;                            // kFineChunk, sorted by fine bucket
-    uint8_t *sf = reinterpret_cast<uint8_t *>(stage + kFineChunk); // kFineChunk fine ids
+    // kFineGather gathered tuples; a chunk is staged, sorted by fine bucket, in
+    // its own part of it (its tuples are in registers by then)
+    uint64_t *tmp = reinterpret_cast<uint64_t *>(smem_raw);
+    uint8_t *sf = reinterpret_cast<uint8_t *>(tmp + kFineGather);   // kFineChunk fine ids
     __shared__ uint32_t runoff[kGroupTiles], runpre[kGroupTiles + 1];
     __shared__ uint32_t fcnt[kCoarseMax], floc[kCoarseMax], fbase[kCoarseMax];
     __shared__ LearnedCore core;
@@ -863,11 +887,8 @@ __device__ __forceinline__ void fine_item(const WorkItem it, const WinPlan *__re
     const WinPlan wp = wins[w];
     const LearnedModel *gm = model_of(wp, models);   // a two-level window that was not compacted
     const uint32_t lg = wp.log2_buckets, lgC = coarse_bits(lg), cshift = lg - lgC, nfine = 1u << cshift;
-    const uint32_t ntw = tp[w + 1] - tp[w];
-    const uint32_t ngroups = (ntw + kGroupTiles - 1) / kGroupTiles;
-    const uint32_t local = it.local;
-    const uint32_t c = local / ngroups, g = local % ngroups;
-    const uint32_t t0 = g * kGroupTiles, G = min(kGroupTiles, ntw - t0);
+    const FineRuns fr_it = fine_runs(it, wins, tileL, tileR);
+    const uint32_t c = fr_it.c, t0 = fr_it.t0, G = fr_it.G;
     const Classifier cls = make_classifier(wp, gm, core);   // ends with a barrier when there is a model
     const uint32_t *rows_side = rows + (right ? tileL[nwin] : 0) * kRow;
     if (warp_id() == 0) {
@@ -902,65 +923,70 @@ __device__ __forceinline__ void fine_item(const WorkItem it, const WinPlan *__re
     uint32_t *gcur = cursor + (right ? B : 0) + wp.bucket_base + (c << cshift);
     constexpr int kPer = kFineChunk / kFineThreads;
     const uint32_t nwarps = blockDim.x >> 5;
-    for (uint32_t ch = 0; ch < T; ch += kFineChunk) {
-        const uint32_t m = min(kFineChunk, T - ch);
-        for (uint32_t f = threadIdx.x; f < nfine; f += blockDim.x) fcnt[f] = 0;
-        // gather: warp r % nwarps copies the part of run r inside [ch, ch + m)
+    for (uint32_t gw = 0; gw < T; gw += kFineGather) {
+        const uint32_t mg = min(kFineGather, T - gw);
+        // gather: warp r % nwarps copies the part of run r inside [gw, gw + mg)
         for (uint32_t r = warp_id(); r < G; r += nwarps) {
-            const uint32_t a = max(runpre[r], ch), b = min(runpre[r + 1], ch + m);
+            const uint32_t a = max(runpre[r], gw), b = min(runpre[r + 1], gw + mg);
             for (uint32_t x = a + lane_id(); x < b; x += 32)
-                cp_async8(tmp + (x - ch), src + runoff[r] + (x - runpre[r]));
+                cp_async8(tmp + (x - gw), src + runoff[r] + (x - runpre[r]));
         }
         cp_async_wait_all();
         SJBG_BARRIER();
-        uint64_t e[kPer];
-        uint32_t fr[kPer];
+        for (uint32_t ch = 0; ch < mg; ch += kFineChunk) {
+            const uint32_t m = min(kFineChunk, mg - ch);
+            uint64_t *stage = tmp + ch;
+            for (uint32_t f = threadIdx.x; f < nfine; f += blockDim.x) fcnt[f] = 0;
+            SJBG_BARRIER();
+            uint64_t e[kPer];
+            uint32_t fr[kPer];
 #pragma unroll
-        for (int k = 0; k < kPer; k++) {
-            const uint32_t j = threadIdx.x + k * kFineThreads;
-            fr[k] = 0xFFFFFFFFu;
-            if (j < m) {
-                e[k] = tmp[j];
-                const uint32_t f = cls.bucket((uint32_t)e[k]) & (nfine - 1);
-                fr[k] = (f << 16) | atomicAdd(&fcnt[f], 1u);
-            }
-        }
-        SJBG_BARRIER();
-        if (warp_id() == 0) {
-            uint32_t a[kCoarseMax / 32], sum = 0;
-#pragma unroll
-            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
-                const uint32_t f = lane_id() * (kCoarseMax / 32) + q;
-                a[q] = f < nfine ? fcnt[f] : 0u;
-                sum += a[q];
-            }
-            uint32_t tot;
-            uint32_t run = warp_excl_scan(sum, &tot);
-#pragma unroll
-            for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
-                const uint32_t f = lane_id() * (kCoarseMax / 32) + q;
-                if (f < nfine) {
-                    floc[f] = run;
-                    fbase[f] = a[q] ? atomicAdd(&gcur[f], a[q]) : 0u;
+            for (int k = 0; k < kPer; k++) {
+                const uint32_t j = threadIdx.x + k * kFineThreads;
+                fr[k] = 0xFFFFFFFFu;
+                if (j < m) {
+                    e[k] = tmp[ch + j];
+                    const uint32_t f = cls.bucket((uint32_t)e[k]) & (nfine - 1);
+                    fr[k] = (f << 16) | atomicAdd(&fcnt[f], 1u);
                 }
-                run += a[q];
             }
-        }
-        SJBG_BARRIER();
+            SJBG_BARRIER();
+            if (warp_id() == 0) {
+                uint32_t a[kCoarseMax / 32], sum = 0;
 #pragma unroll
-        for (int k = 0; k < kPer; k++) {
-            if (fr[k] != 0xFFFFFFFFu) {
-                const uint32_t pos = floc[fr[k] >> 16] + (fr[k] & 0xFFFFu);
-                stage[pos] = e[k];
-                sf[pos] = (uint8_t)(fr[k] >> 16);
+                for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                    const uint32_t f = lane_id() * (kCoarseMax / 32) + q;
+                    a[q] = f < nfine ? fcnt[f] : 0u;
+                    sum += a[q];
+                }
+                uint32_t tot;
+                uint32_t run = warp_excl_scan(sum, &tot);
+#pragma unroll
+                for (int q = 0; q < (int)(kCoarseMax / 32); q++) {
+                    const uint32_t f = lane_id() * (kCoarseMax / 32) + q;
+                    if (f < nfine) {
+                        floc[f] = run;
+                        fbase[f] = a[q] ? atomicAdd(&gcur[f], a[q]) : 0u;
+                    }
+                    run += a[q];
+                }
             }
+            SJBG_BARRIER();
+#pragma unroll
+            for (int k = 0; k < kPer; k++) {
+                if (fr[k] != 0xFFFFFFFFu) {
+                    const uint32_t pos = floc[fr[k] >> 16] + (fr[k] & 0xFFFFu);
+                    stage[pos] = e[k];
+                    sf[pos] = (uint8_t)(fr[k] >> 16);
+                }
+            }
+            SJBG_BARRIER();
+            for (uint32_t pos = threadIdx.x; pos < m; pos += blockDim.x) {
+                const uint32_t f = sf[pos];
+                out[fbase[f] + (pos - floc[f])] = stage[pos];
+            }
+            SJBG_BARRIER();
         }
-        SJBG_BARRIER();
-        for (uint32_t pos = threadIdx.x; pos < m; pos += blockDim.x) {
-            const uint32_t f = sf[pos];
-            out[fbase[f] + (pos - floc[f])] = stage[pos];
-        }
-        SJBG_BARRIER();
     }
 }
 

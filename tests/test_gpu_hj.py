@@ -94,6 +94,28 @@ def test_edge_cases(lib, oracle, part):
             assert np.array_equal(sorted_pairs(pairs[:got["n_pairs"]]), sorted_pairs(want["pairs"]))
 
 
+@pytest.mark.parametrize("part", ["radix", "learned", "hbm_table"])
+def test_edge_cases_count_mode(lib, oracle, part):
+    """The same edge cases through the count-only kernels (no pairs, no xor):
+    the HBM table's all-ones key lives in its extra slot, a hot key is
+    installed once and then added to, and a warp's equal keys are combined."""
+    p = getattr(lib, PARTS[part])
+    cases = [
+        ([], []), ([1, 2, 3], []), ([], [4]), ([5], [5]),
+        ([7] * 3000, [7] * 2000),
+        ([0xFFFFFFFF, 0, 0xFFFFFFFF, 9], [0xFFFFFFFF, 9, 9]),
+        ([0xFFFFFFFF] * 700 + [0] * 300, [0] * 5 + [0xFFFFFFFF] * 11),
+        (list(range(10000)), list(range(5000, 15000))),
+        ([3] * 5000 + list(range(100, 9000)), [3] * 3000 + list(range(50, 7000))),
+    ]
+    with lib.Joiner(lib.ALG_HJ, lib.LAZY, lib.RESULT_NO_OUTPUT, partitioner=p, max_tuples_per_window=1 << 16) as j:
+        for kl, kr in cases:
+            l, r = make_tuples(kl), make_tuples(kr, first=len(kl))
+            want = oracle.join(l, r, enumerate_pairs=False)
+            got = j.lazy_execute(l, r)
+            assert (got["count"], got["prod"]) == (want["count"], want["prod"]), (kl[:5], kr[:5])
+
+
 def test_skewed_count_mode_overflow_passes(lib, oracle):
     """Buckets with more distinct keys than a shared table holds are joined in several passes."""
     n = 1 << 18
