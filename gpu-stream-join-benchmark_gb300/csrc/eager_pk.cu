@@ -412,6 +412,16 @@ __device__ __forceinline__ uint32_t warp_search(const uint32_t *a, uint32_t n, u
     return lo + __popc(__ballot_sync(0xFFFFFFFFu, before));
 }
 
+// Upper bound of key in sorted a[lo, n) when a[lo] starts key's run (lo is its
+// lower bound): one round of 32 probes when the run is shorter than 32 (the
+// common case), the full search past them otherwise.
+__device__ __forceinline__ uint32_t warp_upper_from(const uint32_t *a, uint32_t n, uint32_t lo, uint32_t key) {
+    const uint32_t p = lo + lane_id();
+    const unsigned le = __ballot_sync(0xFFFFFFFFu, p < n && a[p] <= key);
+    if (le != 0xFFFFFFFFu) return lo + __popc(le);
+    return lo + 32 + warp_search<true>(a + lo + 32, n - lo - 32, key);
+}
+
 // Phase 0: the batch's (key, val) into device memory, once (every CTA reads
 // all of it next; from the host link that would be once per CTA).
 // Phase 1: rank each batch element in (key, arrival) order with the exclusive
@@ -463,7 +473,7 @@ __device__ void pk_smj_batch(const PkArgs &a, const PkWork &w, uint8_t *smem) {
         }
         // the probe
         const uint32_t lo = warp_search<false>(okeys, w.oth_n, kj);
-        const uint32_t hi = (lo < w.oth_n && okeys[lo] == kj) ? warp_search<true>(okeys, w.oth_n, kj) : lo;
+        const uint32_t hi = (lo < w.oth_n && okeys[lo] == kj) ? warp_upper_from(okeys, w.oth_n, lo, kj) : lo;
         if (lane == 0) {
             count += hi - lo;
             prod += sh[j] * (oF[hi] - oF[lo]);
@@ -727,9 +737,12 @@ static int pk_init(sjbg_handle *h) {
     }
     // HJ: one tuple per thread of a 4,096-tuple batch (fewer CTAs, fewer arrivals per
     // ticket), the rest of the GPU stays free; NLJ and SMJ: the whole GPU (their
-    // tickets are compare- or bandwidth-heavy)
-    pk->grid = h->cfg.algorithm == SJBG_ALG_HJ ? std::min(16, h->num_sms)
-                                               : std::min(occ, 2) * h->num_sms;
+    // tickets are compare- or bandwidth-heavy).  Measured per ticket: the SMJ at
+    // W = 2^20 takes 52 us with 2 CTAs per SM and 45 us with 4; the NLJ at
+    // W = 65,536 takes 26 us with 2 and 37 us with 4 (its blocks are fewer than
+    // the slots of 4 per SM, and every CTA joins each grid barrier)
+    const int per_sm = h->cfg.algorithm == SJBG_ALG_SMJ ? 4 : 2;
+    pk->grid = h->cfg.algorithm == SJBG_ALG_HJ ? std::min(16, h->num_sms) : std::min(occ, per_sm) * h->num_sms;
     int pageable = 0;
     if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess) {
         cudaGetLastError();
