@@ -144,6 +144,35 @@ int zero_fill(sjbg_handle *h, void *dst, size_t bytes) {
     return SJBG_OK;
 }
 
+// CTA 0 copies the staged bytes (16-byte words when both sides allow); every
+// CTA zeroes its share of zdst.
+__global__ void stage_copy_zero_kernel(uint8_t *__restrict__ dst, const uint8_t *__restrict__ src, size_t bytes,
+                                       bool vec, uint4 *__restrict__ zdst, size_t n16) {
+    if (blockIdx.x == 0) {
+        if (vec) {
+            for (size_t i = threadIdx.x; i < (bytes + 15) / 16; i += blockDim.x)
+                reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+        } else {
+            for (size_t i = threadIdx.x; i < bytes; i += blockDim.x) dst[i] = src[i];
+        }
+    }
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += stride) zdst[i] = make_uint4(0, 0, 0, 0);
+}
+
+int stage_copy_zero(sjbg_handle *h, void *dst, const void *src, size_t bytes, void *zdst, size_t zbytes) {
+    const size_t n16 = (zbytes + 15) / 16;
+    if (bytes == 0) return zero_fill(h, zdst, zbytes);
+    if (n16 == 0) return stage_copy(h, dst, src, bytes);
+    const bool vec = (((uintptr_t)dst | (uintptr_t)src) & 15u) == 0;
+    const uint32_t blocks =
+        (uint32_t)std::min<size_t>((n16 + 255) / 256, (size_t)8 * (size_t)std::max(h->num_sms, 1));
+    SJBG_CK(h, launch(h, "stage_copy_zero", stage_copy_zero_kernel, dim3(std::max<uint32_t>(blocks, 1)), dim3(256), 0,
+                      static_cast<uint8_t *>(dst), static_cast<const uint8_t *>(src), bytes, vec,
+                      static_cast<uint4 *>(zdst), n16));
+    return SJBG_OK;
+}
+
 int stage_copy(sjbg_handle *h, void *dst, const void *src, size_t bytes) {
     if (bytes == 0) return SJBG_OK;
     const bool vec = (((uintptr_t)dst | (uintptr_t)src) & 15u) == 0;

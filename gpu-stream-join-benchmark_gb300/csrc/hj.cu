@@ -1624,7 +1624,10 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     std::memcpy(hst + planB + 8 * tileB, bwin.data(), bwB);
     LearnedStage lst{};
     if (learned) lst = learned_stage(h, plan.data(), n, hst + lsOff);
-    if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
+    // the bucket counters are zeroed by the same launch as the upload
+    uint32_t *dCnt = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CNT, sizeof(uint32_t) * 2 * B));
+    if (!dCnt) return fail(h, SJBG_E_NOMEM, "partition buffers");
+    if (int rc_up = stage_copy_zero(h, dev, hst, upB, dCnt, sizeof(uint32_t) * 2 * B)) return rc_up;
     WinPlan *dPlan = reinterpret_cast<WinPlan *>(dev);
     const uint32_t *dTileL = reinterpret_cast<const uint32_t *>(dev + planB);
     const uint32_t *dTileR = reinterpret_cast<const uint32_t *>(dev + planB + tileB);
@@ -1636,7 +1639,6 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     const uint32_t *dPbR = reinterpret_cast<const uint32_t *>(dev + planB + 7 * tileB);
     const uint32_t *dBwin = reinterpret_cast<const uint32_t *>(dev + planB + 8 * tileB);
 
-    uint32_t *dCnt = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CNT, sizeof(uint32_t) * 2 * B));
     uint32_t *dStart = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_START, sizeof(uint32_t) * 2 * B));
     uint32_t *dCur = static_cast<uint32_t *>(ws_get(h, WS_BUCKET_CURSOR, sizeof(uint32_t) * 2 * B));
     uint64_t *dPL = static_cast<uint64_t *>(ws_get(h, WS_PART_LEFT, sizeof(uint64_t) * std::max<uint64_t>(totL, 1)));
@@ -1670,7 +1672,6 @@ int hj_lazy_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, co
     SJBG_CK(h, cudaMemsetAsync(dCcnt, 0, sizeof(uint32_t) * (2 * n + 1), h->stream));
     uint64_t *dCompR = dComp + (uint64_t)kTile * tileL[n];
 
-    SJBG_CK(h, cudaMemsetAsync(dCnt, 0, sizeof(uint32_t) * 2 * B, h->stream));
     const uint32_t tiles = tileL[n] + tileR[n];
     if (tiles) {
         const size_t histSmem = sizeof(uint32_t) * ((maxP + 1) / 2 * 2) + sizeof(uint64_t) * kTile;

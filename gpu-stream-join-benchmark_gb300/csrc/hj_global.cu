@@ -380,8 +380,7 @@ int hj_global_batch(sjbg_handle *h, const sjbg_tuple *dL, const sjbg_tuple *dR, 
     std::memcpy(hst, gw.data(), gwB);
     std::memcpy(hst + gwB, tl.data(), tB);
     std::memcpy(hst + gwB + tB, tr.data(), tB);
-    if (int rc_up = stage_copy(h, dev, hst, upB)) return rc_up;
-    if (int rc_z = zero_fill(h, dTab, slotB * slots)) return rc_z;
+    if (int rc_up = stage_copy_zero(h, dev, hst, upB, dTab, slotB * slots)) return rc_up;
     const GWin *dW = reinterpret_cast<const GWin *>(dev);
     const uint32_t *dTl = reinterpret_cast<const uint32_t *>(dev + gwB);
     const uint32_t *dTr = reinterpret_cast<const uint32_t *>(dev + gwB + tB);

@@ -112,6 +112,9 @@ int stage_copy(sjbg_handle *h, void *dst, const void *src, size_t bytes);
 // zeros stay in L2 for the kernels that use the buffer next, where a memset
 // may write them past L2.
 int zero_fill(sjbg_handle *h, void *dst, size_t bytes);
+// stage_copy and zero_fill in one launch (a call's plan upload and its table
+// clear: one kernel boundary less on the call's critical path).
+int stage_copy_zero(sjbg_handle *h, void *dst, const void *src, size_t bytes, void *zdst, size_t zbytes);
 
 // Device buffer of at least `bytes` in slot s (contents not preserved on growth).
 void *ws_get(sjbg_handle *h, WsSlot s, size_t bytes);
