@@ -11,12 +11,17 @@
 //                    -> one atomicAdd per non-empty bucket into the global counts.
 //   2. part_scan     per window, exclusive scan of its counts on both sides ->
 //                    bucket starts; buckets with tuples on both sides form the
-//                    join list, the only buckets step 4 visits.
+//                    join list (item records), the only buckets step 4 visits.
 //   3. part_scatter  per tile: local counting sort by bucket in shared memory,
 //                    one atomicAdd per bucket to reserve a range, then the tile
-//                    is written as contiguous per-bucket runs of (key,val) words.
-//   4. bucket_join   one CTA per (window, bucket): build an open-addressing table
-//                    in shared memory from the left run, probe with the right run.
+//                    is written as contiguous per-bucket runs of (key,val) words
+//                    (windows of many buckets: a coarse pass inside part_hist,
+//                    then part_fine).
+//   4. bucket_join   per join item (persistent CTAs, one item ahead): a radix
+//                    window's bucket through a direct table indexed by
+//                    key >> radix bits when its indices allow it, else an
+//                    open-addressing table in shared memory from the left run,
+//                    probed with the right run.
 //        count mode: table slot = {key, count, sum fr(val)}, updated with
 //                    32-bit shared atomics (the sum as two words with carry);
 //                    keys that do not fit go back into the left run (compacted
