@@ -269,8 +269,7 @@ rs_scan_kernel(uint32_t *__restrict__ counts, const SortSeg *__restrict__ segs, 
 struct DownSmem {
     uint32_t in_keys[kSortTile];
     uint32_t in_vals[kSortTile];
-    uint32_t out_keys[kSortTile];
-    uint32_t out_vals[kSortTile];
+    uint16_t perm[kSortTile];                  // tile position of the p-th element in sorted order
     uint32_t wcnt[kSortWarps][kDigits + 1];   // per-warp digit counters (+1: invalid slots)
     uint32_t loc[kDigits];                     // tile-local digit offsets
     uint32_t gofs[kDigits];                    // global digit offsets of this tile
@@ -278,7 +277,9 @@ struct DownSmem {
     uint64_t bar;
 };
 
-__global__ void __launch_bounds__(kSortThreads)
+// Three CTAs per SM: the reorder keeps a 16-bit permutation instead of a
+// second copy of the tile's keys and vals (58 KB of shared memory per CTA).
+__global__ void __launch_bounds__(kSortThreads, 3)
 rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
                     const SortSeg *__restrict__ segs, const uint32_t *__restrict__ tile_seg, uint32_t shift,
@@ -363,17 +364,17 @@ rs_downsweep_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restric
         if (pos < n) {
             const uint32_t d = dig[k];
             const uint32_t p = sm.loc[d] + sm.wcnt[w][d] + rank[k];
-            sm.out_keys[p] = sm.in_keys[pos];
-            sm.out_vals[p] = sm.in_vals[pos];
+            sm.perm[p] = (uint16_t)pos;
         }
     }
     SJBG_BARRIER();
     for (uint32_t j = threadIdx.x; j < n; j += kSortThreads) {
-        const uint32_t k = sm.out_keys[j];
+        const uint32_t q = sm.perm[j];
+        const uint32_t k = sm.in_keys[q];
         const uint32_t d = (k >> shift) & 0xFFu;
         const uint64_t dst = sg.off + sm.gofs[d] + (j - sm.loc[d]);
         keys_out[dst] = k;
-        vals_out[dst] = sm.out_vals[j];
+        vals_out[dst] = sm.in_vals[q];
     }
 }
 
