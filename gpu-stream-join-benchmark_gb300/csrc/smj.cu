@@ -141,7 +141,7 @@ merge_join_kernel(const SortView *__restrict__ view, const unsigned long long *_
                 lo = l3;
             }
             count += hi - lo;
-            prod += (Fa[hi] - Fa[lo]) * sjbg_gs(bval);
+            if (hi > lo) prod += (Fa[hi] - Fa[lo]) * sjbg_gs(bval);   // (no prefix loads without a match)
             if (kEnum)
                 for (uint32_t a = lo; a < hi; a++) xr ^= sjbg_pair_hash(Av[a], bval);
         }
