@@ -108,12 +108,23 @@ merge_join_kernel(const SortView *__restrict__ view, const unsigned long long *_
     sjbg_pair *pout = kPairs ? pairs + mw.pairs_off : nullptr;
 
     unsigned long long count = 0, prod = 0, xr = 0;
+    // the next B element's key and val are loaded while this one is searched
+    uint32_t nkey = 0, nval = 0;
+    if (j0 + threadIdx.x < j1) {
+        nkey = B[j0 + threadIdx.x];
+        nval = Bv[j0 + threadIdx.x];
+    }
     for (uint32_t jb = j0; jb < j1; jb += kMergeThreads) {   // uniform trip count (warp collectives below)
         const uint32_t j = jb + threadIdx.x;
         uint32_t lo = 0, hi = 0, bval = 0;
+        const uint32_t ckey = nkey, cval = nval;
+        if (j + kMergeThreads < j1) {
+            nkey = B[j + kMergeThreads];
+            nval = Bv[j + kMergeThreads];
+        }
         if (j < j1) {
-            const uint32_t key = B[j];
-            bval = Bv[j];
+            const uint32_t key = ckey;
+            bval = cval;
             // hi: first A position in the tile with A > key
             uint32_t l = 0, r = m;
             while (l < r) {
