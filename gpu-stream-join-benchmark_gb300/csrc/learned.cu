@@ -166,8 +166,13 @@ constexpr uint32_t kNoKey = 0xFFFFFFFFu;   // empty shared slot (the key itself 
 constexpr uint32_t kCountPer = kCountChunk / kSampleThreads;   // keys per thread and chunk
 static_assert(kCountChunk % kSampleThreads == 0 && kCountSlots + 1 <= 0xFFFFu, "chunk layout");
 
-__device__ __forceinline__ void count_update(const SampleWin &s, SampleScratch &sc, uint32_t *hw,
-                                             unsigned long long *tw, uint32_t *lw, float kmin, float inv, uint32_t k,
+// The count-class changes and the newly listed slots of a CTA's chunk are
+// gathered in shared memory and added to the window's counters once per chunk
+// (cls_d: per class, the change; list_s / n_list_s: the slots that reached
+// thresh): every CTA of a window updates the same few class counters, and one
+// global atomic per change serialised there.
+__device__ __forceinline__ void count_update(const SampleWin &s, uint32_t *hw, unsigned long long *tw, int *cls_d,
+                                             uint32_t *list_s, uint32_t *n_list_s, float kmin, float inv, uint32_t k,
                                              uint32_t c) {
     const uint32_t mask = (1u << s.table_log2) - 1;
     atomicAdd(&hw[bin_of(key_x(k, kmin, inv))], c);
@@ -192,14 +197,13 @@ __device__ __forceinline__ void count_update(const SampleWin &s, SampleScratch &
     if (before == 0xFFFFFFFFu || after < s.thresh) return;   // (a full table drops the key)
     const int cn = 31 - __clz(after);
     if (before < s.thresh) {
-        atomicAdd(&sc.cls[cn], 1u);
-        const uint32_t pos = atomicAdd(&sc.n_list, 1u);
-        if (pos < s.list_cap) lw[pos] = slot;
+        atomicAdd(&cls_d[cn], 1);
+        list_s[atomicAdd(n_list_s, 1u)] = slot;   // at most one per distinct key of the chunk
     } else {
         const int co = 31 - __clz(before);
         if (co != cn) {
-            atomicAdd(&sc.cls[cn], 1u);
-            atomicSub(&sc.cls[co], 1u);
+            atomicAdd(&cls_d[cn], 1);
+            atomicSub(&cls_d[co], 1);
         }
     }
 }
@@ -210,6 +214,9 @@ sample_count_kernel(const uint32_t *keys, const SampleWin *wins, SampleScratch *
     __shared__ uint32_t skey[kCountSlots], scnt[kCountSlots + 1];
     __shared__ uint16_t used[kCountChunk + 1];   // slots taken by the chunk's distinct keys
     __shared__ uint32_t n_used;
+    __shared__ int cls_d[32];                     // the chunk's count-class changes
+    __shared__ uint32_t list_s[kCountChunk + 1];  // the chunk's newly listed table slots
+    __shared__ uint32_t n_list_s, list_base;
     const uint32_t w = blockIdx.y;
     const SampleWin s = wins[w];
     float kmin, inv;
@@ -223,7 +230,11 @@ sample_count_kernel(const uint32_t *keys, const SampleWin *wins, SampleScratch *
         if (j < kCountSlots) skey[j] = kNoKey;
         scnt[j] = 0;
     }
-    if (threadIdx.x == 0) n_used = 0;
+    if (threadIdx.x == 0) {
+        n_used = 0;
+        n_list_s = 0;
+    }
+    if (threadIdx.x < 32) cls_d[threadIdx.x] = 0;
     SJBG_BARRIER();
     for (uint32_t base = blockIdx.x * kCountChunk; base < s.m; base += gridDim.x * kCountChunk) {
         const uint32_t end = min(base + kCountChunk, s.m);
@@ -264,13 +275,27 @@ sample_count_kernel(const uint32_t *keys, const SampleWin *wins, SampleScratch *
         const uint32_t nu = n_used;
         for (uint32_t u = threadIdx.x; u < nu; u += blockDim.x) {
             const uint32_t j = used[u];
-            count_update(s, sc, hw, tw, lw, kmin, inv, j < kCountSlots ? skey[j] : kNoKey, scnt[j]);
+            count_update(s, hw, tw, cls_d, list_s, &n_list_s, kmin, inv, j < kCountSlots ? skey[j] : kNoKey,
+                         scnt[j]);
             if (j < kCountSlots) skey[j] = kNoKey;
             scnt[j] = 0;
         }
         SJBG_BARRIER();
-        if (threadIdx.x == 0) n_used = 0;
+        // the chunk's class changes and listed slots into the window's counters and list
+        if (threadIdx.x < 32 && cls_d[threadIdx.x] != 0) {
+            atomicAdd(&sc.cls[threadIdx.x], (uint32_t)cls_d[threadIdx.x]);   // (a negative change wraps)
+            cls_d[threadIdx.x] = 0;
+        }
+        const uint32_t nl = n_list_s;
+        if (threadIdx.x == 0) {
+            list_base = nl ? atomicAdd(&sc.n_list, nl) : 0u;
+            n_used = 0;
+        }
         SJBG_BARRIER();
+        for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x)
+            if (list_base + i < s.list_cap) lw[list_base + i] = list_s[i];
+        SJBG_BARRIER();
+        if (threadIdx.x == 0) n_list_s = 0;
     }
 }
 
