@@ -201,6 +201,22 @@ def _line(metric, value, unit, ms, args, workload, extra, higher=True):
 _FLUSH = {}
 
 
+def replica_first_tuple(rank, nwin, W):
+    """Multi-GPU form (replicas only): rank r joins its own nwin windows of W
+    tuples per stream, the r-th block of the stream (windows are independent
+    units, so no tuple crosses ranks and no collective is on the data path)."""
+    return rank * nwin * W
+
+
+def max_over_ranks(torch, ms, world, device="cuda"):
+    """A step's time over all ranks: the slowest rank's (the job's time)."""
+    if world <= 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def l2_flush(torch, stream):
     """Write 256 MiB (about twice the 129 MB L2) on `stream`, so that the next
     step starts with none of its inputs in L2."""
@@ -943,7 +959,7 @@ def main():
     plain_bits = 10 if W >= (1 << 20) else 0
     gen = sjbg.Joiner(**flags_common)
     # each rank joins its own windows (weak scaling: windows are independent)
-    first = rank * total
+    first = replica_first_tuple(rank, nwin, W)
     gen.generate(dL.data_ptr(), first, total, 1, D, table_ptr, 3)
     gen.generate(dR.data_ptr(), first, total, 2, D, table_ptr, 3)
     gen.close()
@@ -1002,10 +1018,7 @@ def main():
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / k
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(torch, ms, world)
         return ms, [(r.count, r.prod_checksum, r.partitioner_used, r.flags) for r in res]
 
     launches0 = learned.launch_count()
